@@ -1,0 +1,26 @@
+/*
+ * chunk_extension.h -- what the GB300 backend adds to TeaLeaf's Chunk.
+ *
+ * Found by the driver through the include path (the reference driver
+ * includes it from chunk.h:7). FieldBufferType is a device pointer: the
+ * host never dereferences fields. The extension holds the backend context
+ * and the state of the run-ahead CG mode (see kernel_interface.cpp).
+ */
+#pragma once
+
+typedef double* FieldBufferType;
+
+struct tl_context;
+
+typedef struct ChunkExtension {
+  struct tl_context* ctx;
+  double* comms_buffer;   /* unused: halo staging lives in the context */
+  int fused_cg;           /* 1: run_cg_init runs the whole solve on the device */
+  int ra_active;          /* run-ahead replay in progress */
+  int ra_steps;           /* CG steps executed by the device solve */
+  int ra_k;               /* next step the driver will ask for */
+  double ra_rro0;         /* initial r.p of the device solve */
+  double* ra_pw;          /* host: pw of each device step */
+  double* ra_rrn;         /* host: rrn of each device step */
+  int ra_cap;
+} ChunkExtension;

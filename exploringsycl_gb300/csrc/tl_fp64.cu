@@ -1,0 +1,1095 @@
+/*
+ * tl_fp64.cu -- double-precision kernels of the GB300 TeaLeaf backend: the
+ * drop-in replacements of the reference's SYCL kernels and the persistent
+ * CG solve. Compiled with --fmad=false: every product and sum is rounded
+ * separately, as a sequential evaluation of the reference's expressions
+ * would round it, so the results match the CPU oracle bit for bit.
+ *
+ * Launch shapes
+ *  - map kernels: 256 threads, one cell per thread, grid-stride;
+ *  - reducing kernels: 256 threads (8 warps) per 4096-cell tile, one warp per
+ *    64-cell group; the last block to finish reduces the tile partials in
+ *    the reference order and writes the scalar straight into pinned host
+ *    memory, so one launch and one stream synchronisation return a dot
+ *    product (the reference issues 1 + ceil(log64 n) kernels and a blocking
+ *    host read, TeaLeaf/c_kernels/sycl/sycl_shared.hpp:35-79);
+ *  - the persistent CG kernel: one 512-thread block per SM (cooperative
+ *    launch), three grid barriers per CG step, scalars alpha/beta computed
+ *    redundantly (and identically) by every block.
+ */
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+
+#include "tl_internal.cuh"
+
+namespace {
+
+constexpr int kMapThreads = 256;
+constexpr int kRedThreads = 256;
+constexpr int kPersistThreads = 512;
+
+/* ------------------------------------------------------------ helpers */
+
+__device__ __forceinline__ bool interior(int kk, int jj, int x, int y, int hd) {
+  return kk >= hd && kk < x - hd && jj >= hd && jj < y - hd;
+}
+
+/* The 5-point operator of TeaLeaf/shared.h:59-63 with the reference's
+ * grouping: ((1 + (kx1+kx0)) + (ky1+ky0))*a - (kx1*a1 + kx0*a-1)
+ * - (ky1*a+x + ky0*a-x). */
+template <class Load>
+__device__ __forceinline__ double smvp(Load a, const double* __restrict__ kx,
+                                       const double* __restrict__ ky,
+                                       unsigned i, int x) {
+  const double kx0 = kx[i], kx1 = kx[i + 1];
+  const double ky0 = ky[i], ky1 = ky[i + x];
+  return (1.0 + (kx1 + kx0) + (ky1 + ky0)) * a(i) -
+         (kx1 * a(i + 1) + kx0 * a(i - 1)) -
+         (ky1 * a(i + x) + ky0 * a(i - x));
+}
+
+struct PlainLoad {
+  const double* p;
+  __device__ __forceinline__ double operator()(unsigned i) const { return p[i]; }
+};
+
+/* Loads that bypass L1: for fields that other blocks of the same
+ * persistent kernel rewrite between grid barriers. */
+struct L2Load {
+  const double* p;
+  __device__ __forceinline__ double operator()(unsigned i) const { return __ldcg(p + i); }
+};
+
+/* ---------------------------------------------------------- map kernels */
+
+template <class Op>
+__global__ void __launch_bounds__(kMapThreads) map_kernel(Op op, int x, int y) {
+  const unsigned len = (unsigned)x * (unsigned)y;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += gridDim.x * blockDim.x) {
+    const int jj = (int)(i / (unsigned)x);
+    const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+    op(i, kk, jj);
+  }
+}
+
+template <class Op>
+int launch_map(tl_context* ctx, const Op& op, int x, int y) {
+  const unsigned len = (unsigned)x * (unsigned)y;
+  unsigned blocks = (len + kMapThreads - 1) / kMapThreads;
+  const unsigned cap = (unsigned)ctx->num_sms * 16u;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  map_kernel<Op><<<blocks, kMapThreads, 0, ctx->stream>>>(op, x, y);
+  TL_CHECK_LAUNCH(ctx);
+  return TL_OK;
+}
+
+/* ----------------------------------------------------- reducing kernels */
+
+/* Op must provide `static constexpr int N` (number of sums) and
+ * `operator()(i, kk, jj, double* c)` that, for an interior cell, performs
+ * the cell's update and stores its N contributions into c. */
+template <class Op>
+__global__ void __launch_bounds__(kRedThreads)
+reduce_kernel(Op op, int x, int y, int hd, double* part, size_t part_stride,
+              int ntiles, unsigned* ticket, double* result) {
+  constexpr int N = Op::N;
+  __shared__ double s_group[N][TL_GROUP];
+  __shared__ double s_scratch[TL_RED_SCRATCH];
+  __shared__ int s_last;
+  const unsigned len = (unsigned)x * (unsigned)y;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const unsigned base = (unsigned)tile * TL_TILE;
+    for (int g = warp; g < TL_GROUP; g += nwarps) {
+      const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
+      double c0[N], c1[N];
+#pragma unroll
+      for (int s = 0; s < N; ++s) { c0[s] = 0.0; c1[s] = 0.0; }
+      if (i0 < len) {
+        const int jj = (int)(i0 / (unsigned)x);
+        const int kk = (int)(i0 - (unsigned)jj * (unsigned)x);
+        if (interior(kk, jj, x, y, hd)) op(i0, kk, jj, c0);
+      }
+      if (i0 + 1 < len) {
+        const unsigned i1 = i0 + 1;
+        const int jj = (int)(i1 / (unsigned)x);
+        const int kk = (int)(i1 - (unsigned)jj * (unsigned)x);
+        if (interior(kk, jj, x, y, hd)) op(i1, kk, jj, c1);
+      }
+#pragma unroll
+      for (int s = 0; s < N; ++s) {
+        const double v = tl_tree64(c0[s], c1[s]);
+        if (lane == 0) s_group[s][g] = v;
+      }
+    }
+    __syncthreads();
+    if (warp < N) {
+      const double v = tl_tree64(s_group[warp][2 * lane], s_group[warp][2 * lane + 1]);
+      if (lane == 0) part[warp * part_stride + tile] = v;
+    }
+    __syncthreads();
+  }
+
+  /* Last block to finish reduces the tile partials. */
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int s = 0; s < N; ++s) {
+    const double total = tl_reduce_partials(part + s * part_stride, ntiles, s_scratch);
+    if (threadIdx.x == 0) result[s] = total;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence_system();
+    *ticket = 0u;
+  }
+}
+
+/* Launches a reducing kernel and returns its N sums in out[0..N). */
+template <class Op>
+int launch_reduce(tl_context* ctx, const Op& op, int x, int y, int hd,
+                  double* out) {
+  const size_t ntiles = tl_num_tiles(x, y);
+  int rc = tl_ensure_partials(ctx, ntiles);
+  if (rc != TL_OK) return rc;
+  const int blocks = (int)ntiles;
+  reduce_kernel<Op><<<blocks, kRedThreads, 0, ctx->stream>>>(
+      op, x, y, hd, ctx->d_part, ctx->part_cap, (int)ntiles,
+      ctx->d_sync + TL_SYNC_TICKET, ctx->d_result);
+  TL_CHECK_LAUNCH(ctx);
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int s = 0; s < Op::N; ++s) out[s] = ((volatile double*)ctx->h_result)[s];
+  return TL_OK;
+}
+
+/* ------------------------------------------------------------ kernels */
+
+struct CgInitUOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:7-37 */
+  int coefficient;
+  double *p, *r, *u, *w;
+  const double *density, *energy;
+  int x, y;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    p[i] = 0.0;
+    r[i] = 0.0;
+    u[i] = energy[i] * density[i];
+    if (jj > 0 && jj < y - 1 && kk > 0 && kk < x - 1) {
+      w[i] = (coefficient == TL_CONDUCTIVITY) ? density[i] : 1.0 / density[i];
+    }
+  }
+};
+
+struct CgInitKOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:40-69 */
+  int x, y, hd;
+  const double* w;
+  double *kx, *ky;
+  double rx, ry;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (jj >= hd && jj < y - 1 && kk >= hd && kk < x - 1) {
+      kx[i] = rx * (w[i - 1] + w[i]) / (2.0 * w[i - 1] * w[i]);
+      ky[i] = ry * (w[i - x] + w[i]) / (2.0 * w[i - x] * w[i]);
+    }
+  }
+};
+
+struct CgInitOthersOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:72-134 */
+  static constexpr int N = 1;
+  int x;
+  const double *kx, *ky, *u;
+  double *p, *r, *w;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    const double s = smvp(PlainLoad{u}, kx, ky, i, x);
+    w[i] = s;
+    const double rv = u[i] - s;
+    r[i] = rv;
+    p[i] = rv;
+    c[0] = rv * rv;
+  }
+};
+
+struct CgCalcWOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:137-195 */
+  static constexpr int N = 1;
+  int x;
+  const double *p, *kx, *ky;
+  double* w;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    const double s = smvp(PlainLoad{p}, kx, ky, i, x);
+    w[i] = s;
+    c[0] = s * p[i];
+  }
+};
+
+struct CgCalcUrOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:198-254 */
+  static constexpr int N = 1;
+  double *u, *r;
+  const double *p, *w;
+  double alpha;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    u[i] = u[i] + alpha * p[i];
+    const double rv = r[i] - alpha * w[i];
+    r[i] = rv;
+    c[0] = rv * rv;
+  }
+};
+
+struct CgCalcPOp {  /* TeaLeaf/c_kernels/sycl/cg.cpp:257-281 */
+  int x, y, hd;
+  double beta;
+  double* p;
+  const double* r;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) p[i] = beta * p[i] + r[i];
+  }
+};
+
+struct CopyUOp {  /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:7-31 */
+  int x, y, hd;
+  const double* u;
+  double* u0;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) u0[i] = u[i];
+  }
+};
+
+struct ResidualOp {  /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:34-65 */
+  int x, y, hd;
+  const double *u, *u0, *kx, *ky;
+  double* r;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) {
+      const double s = smvp(PlainLoad{u}, kx, ky, i, x);
+      r[i] = u0[i] - s;
+    }
+  }
+};
+
+struct Norm2Op {  /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:68-117 */
+  static constexpr int N = 1;
+  const double* b;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    c[0] = b[i] * b[i];
+  }
+};
+
+struct FinaliseOp {  /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:120-145 */
+  int x, y, hd;
+  const double *u, *density;
+  double* energy;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) energy[i] = u[i] / density[i];
+  }
+};
+
+struct SummaryOp {  /* TeaLeaf/c_kernels/sycl/field_summary.cpp:6-151 */
+  static constexpr int N = 4;
+  const double *u, *density, *energy0, *volume;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    const double cell_vol = volume[i];
+    const double cell_mass = cell_vol * density[i];
+    c[0] = cell_vol;
+    c[1] = cell_mass;
+    c[2] = cell_mass * energy0[i];
+    c[3] = cell_mass * u[i];
+  }
+};
+
+struct InitialStateOp {  /* TeaLeaf/c_kernels/sycl/set_chunk_state.cpp:8-27 */
+  double e, d;
+  double *energy0, *density;
+  __device__ void operator()(unsigned i, int, int) const {
+    energy0[i] = e;
+    density[i] = d;
+  }
+};
+
+struct StateOp {  /* TeaLeaf/c_kernels/sycl/set_chunk_state.cpp:30-92 */
+  int x, y;
+  tl_state s;
+  double *energy0, *density, *u;
+  const double *cell_x, *cell_y, *vertex_x, *vertex_y;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    bool apply = false;
+    if (s.geometry == TL_RECTANGULAR) {
+      apply = vertex_x[kk + 1] >= s.x_min && vertex_x[kk] < s.x_max &&
+              vertex_y[jj + 1] >= s.y_min && vertex_y[jj] < s.y_max;
+    } else if (s.geometry == TL_CIRCULAR) {
+      const double radius = sqrt((cell_x[kk] - s.x_min) * (cell_x[kk] - s.x_min) +
+                                 (cell_y[jj] - s.y_min) * (cell_y[jj] - s.y_min));
+      apply = radius <= s.radius;
+    } else if (s.geometry == TL_POINT) {
+      apply = vertex_x[kk] == s.x_min && vertex_y[jj] == s.y_min;
+    }
+    if (apply) {
+      energy0[i] = s.energy;
+      density[i] = s.density;
+    }
+    if (kk > 0 && kk < x - 1 && jj > 0 && jj < y - 1) u[i] = energy0[i] * density[i];
+  }
+};
+
+struct CopyAllOp {  /* store_energy / jacobi_copy_u: dst = src everywhere */
+  double* dst;
+  const double* src;
+  __device__ void operator()(unsigned i, int, int) const { dst[i] = src[i]; }
+};
+
+struct ChunkDataOp {  /* TeaLeaf/c_kernels/sycl/set_chunk_data.cpp:31-64 */
+  int x, y;
+  const double *vertex_x, *vertex_y;
+  double *cell_x, *cell_y, *volume, *x_area, *y_area;
+  double dx, dy;
+  __device__ void operator()(unsigned i, int, int) const {
+    if (i < (unsigned)x) cell_x[i] = 0.5 * (vertex_x[i] + vertex_x[i + 1]);
+    if (i < (unsigned)y) cell_y[i] = 0.5 * (vertex_y[i] + vertex_y[i + 1]);
+    volume[i] = dx * dy;
+    x_area[i] = dy;
+    y_area[i] = dx;
+  }
+};
+
+__global__ void vertices_kernel(int x, int y, int hd, double* vertex_x,
+                                double* vertex_y, double x_min, double y_min,
+                                double dx, double dy) {
+  /* TeaLeaf/c_kernels/sycl/set_chunk_data.cpp:8-28 */
+  const int n = (x > y ? x : y) + 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < x + 1) vertex_x[i] = x_min + dx * (i - (double)hd);
+    if (i < y + 1) vertex_y[i] = y_min + dy * (i - (double)hd);
+  }
+}
+
+struct JacobiInitOp {  /* TeaLeaf/c_kernels/sycl/jacobi.cpp:7-56 */
+  int x, y, hd, coefficient;
+  double rx, ry;
+  double *u, *u0, *kx, *ky;
+  const double *density, *energy;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (kk > 0 && kk < x - 1 && jj > 0 && jj < y - 1) {
+      const double v = energy[i] * density[i];
+      u0[i] = v;
+      u[i] = v;
+    }
+    if (jj >= hd && jj < y - 1 && kk >= hd && kk < x - 1) {
+      const bool cond = coefficient == TL_CONDUCTIVITY;
+      const double dc = cond ? density[i] : 1.0 / density[i];
+      const double dl = cond ? density[i - 1] : 1.0 / density[i - 1];
+      const double dd = cond ? density[i - x] : 1.0 / density[i - x];
+      kx[i] = rx * (dl + dc) / (2.0 * dl * dc);
+      ky[i] = ry * (dd + dc) / (2.0 * dd * dc);
+    }
+  }
+};
+
+struct JacobiIterateOp {  /* TeaLeaf/c_kernels/sycl/jacobi.cpp:59-119 */
+  static constexpr int N = 1;
+  int x;
+  double* u;
+  const double *u0, *r, *kx, *ky;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    const double v = (u0[i] + (kx[i + 1] * r[i + 1] + kx[i] * r[i - 1]) +
+                      (ky[i + x] * r[i + x] + ky[i] * r[i - x])) /
+                     (1.0 + (kx[i] + kx[i + 1]) + (ky[i] + ky[i + x]));
+    u[i] = v;
+    c[0] = fabs(v - r[i]);
+  }
+};
+
+struct ChebyInitOp {  /* TeaLeaf/c_kernels/sycl/cheby.cpp:7-38 */
+  int x, y, hd;
+  double theta;
+  double *p, *r, *w;
+  const double *u, *u0, *kx, *ky;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) {
+      const double s = smvp(PlainLoad{u}, kx, ky, i, x);
+      w[i] = s;
+      const double rv = u0[i] - s;
+      r[i] = rv;
+      p[i] = rv / theta;
+    }
+  }
+};
+
+struct ChebyIterateOp {  /* TeaLeaf/c_kernels/sycl/cheby.cpp:67-110 */
+  int x, y, hd;
+  double alpha, beta;
+  double *p, *r, *w;
+  const double *u, *u0, *kx, *ky;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) {
+      const double s = smvp(PlainLoad{u}, kx, ky, i, x);
+      w[i] = s;
+      const double rv = u0[i] - s;
+      r[i] = rv;
+      p[i] = alpha * p[i] + beta * rv;
+    }
+  }
+};
+
+struct AddInteriorOp {  /* cheby_calc_u: u += p (cheby.cpp:41-64) */
+  int x, y, hd;
+  const double* p;
+  double* u;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) u[i] = u[i] + p[i];
+  }
+};
+
+struct PpcgInitOp {  /* TeaLeaf/c_kernels/sycl/ppcg.cpp:7-30 */
+  int x, y, hd;
+  double theta;
+  double* sd;
+  const double* r;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) sd[i] = r[i] / theta;
+  }
+};
+
+struct PpcgCalcUrOp {  /* TeaLeaf/c_kernels/sycl/ppcg.cpp:33-63 */
+  int x, y, hd;
+  const double *sd, *kx, *ky;
+  double *r, *u;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) {
+      const double s = smvp(PlainLoad{sd}, kx, ky, i, x);
+      r[i] = r[i] - s;
+      u[i] = u[i] + sd[i];
+    }
+  }
+};
+
+struct PpcgCalcSdOp {  /* TeaLeaf/c_kernels/sycl/ppcg.cpp:66-94 */
+  int x, y, hd;
+  double alpha, beta;
+  double* sd;
+  const double* r;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd)) sd[i] = alpha * sd[i] + beta * r[i];
+  }
+};
+
+/* --------------------------------------------------------------- halos */
+
+constexpr int kMaxHaloFields = 8;
+struct HaloFields {
+  double* f[kMaxHaloFields];
+  int n;
+};
+
+/* Left and right faces (TeaLeaf/c_kernels/sycl/local_halos.cpp:7-54) for
+ * all fields: one thread per (field, row, layer, side). */
+__global__ void halo_lr_kernel(HaloFields hf, int x, int y, int hd, int depth,
+                               int do_left, int do_right) {
+  const long total = (long)hf.n * y * depth * 2;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const int side = (int)(t & 1);
+    long rest = t >> 1;
+    const int flip = (int)(rest % depth);
+    rest /= depth;
+    const int jj = (int)(rest % y);
+    const int fi = (int)(rest / y);
+    double* f = hf.f[fi];
+    if (side == 0 && do_left) {
+      f[(long)jj * x + hd - depth + flip] = f[(long)jj * x + hd + depth - flip - 1];
+    } else if (side == 1 && do_right) {
+      f[(long)jj * x + x - hd + flip] = f[(long)jj * x + x - hd - 1 - flip];
+    }
+  }
+}
+
+/* Top and bottom faces, full rows (local_halos.cpp:57-102). */
+__global__ void halo_tb_kernel(HaloFields hf, int x, int y, int hd, int depth,
+                               int do_bottom, int do_top) {
+  const long total = (long)hf.n * x * depth * 2;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total;
+       t += (long)gridDim.x * blockDim.x) {
+    const int kk = (int)(t % x);
+    long rest = t / x;
+    const int side = (int)(rest & 1);
+    rest >>= 1;
+    const int line = (int)(rest % depth);
+    const int fi = (int)(rest / depth);
+    double* f = hf.f[fi];
+    if (side == 1 && do_top) {
+      f[(long)(y - hd + line) * x + kk] = f[(long)(y - hd - 1 - line) * x + kk];
+    } else if (side == 0 && do_bottom) {
+      f[(long)(hd - 1 - line) * x + kk] = f[(long)(hd + line) * x + kk];
+    }
+  }
+}
+
+int launch_halos(tl_context* ctx, int x, int y, int hd, int depth,
+                 int face_mask, double* const* fields, int nfields) {
+  if (nfields <= 0 || face_mask == 0) return TL_OK;
+  TL_REQUIRE(depth >= 1 && depth <= hd, "halo depth must be in [1, halo_depth]");
+  TL_REQUIRE(x - 2 * hd >= 1 && y - 2 * hd >= 1, "empty interior");
+  const bool L = face_mask & (1 << TL_CHUNK_LEFT), R = face_mask & (1 << TL_CHUNK_RIGHT);
+  const bool B = face_mask & (1 << TL_CHUNK_BOTTOM), T = face_mask & (1 << TL_CHUNK_TOP);
+  for (int f0 = 0; f0 < nfields; f0 += kMaxHaloFields) {
+    HaloFields hf;
+    hf.n = std::min(kMaxHaloFields, nfields - f0);
+    for (int k = 0; k < hf.n; ++k) {
+      TL_REQUIRE(fields[f0 + k] != nullptr, "null halo field");
+      hf.f[k] = fields[f0 + k];
+    }
+    /* Left and right may share a launch only when neither reads a layer
+     * that the other writes (interior at least `depth` wide). */
+    const bool lr_together = (x - 2 * hd) >= depth;
+    const bool tb_together = (y - 2 * hd) >= depth;
+    const long lr_threads = (long)hf.n * y * depth * 2;
+    const long tb_threads = (long)hf.n * x * depth * 2;
+    const int lr_blocks = (int)std::min<long>((lr_threads + 255) / 256, 4096);
+    const int tb_blocks = (int)std::min<long>((tb_threads + 255) / 256, 4096);
+    if (L || R) {
+      if (lr_together || !(L && R)) {
+        halo_lr_kernel<<<lr_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, L, R);
+        TL_CHECK_LAUNCH(ctx);
+      } else {
+        halo_lr_kernel<<<lr_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, 1, 0);
+        TL_CHECK_LAUNCH(ctx);
+        halo_lr_kernel<<<lr_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, 0, 1);
+        TL_CHECK_LAUNCH(ctx);
+      }
+    }
+    if (T || B) {
+      /* Reference order is T then B; they commute when disjoint. */
+      if (tb_together || !(T && B)) {
+        halo_tb_kernel<<<tb_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, B, T);
+        TL_CHECK_LAUNCH(ctx);
+      } else {
+        halo_tb_kernel<<<tb_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, 0, 1);
+        TL_CHECK_LAUNCH(ctx);
+        halo_tb_kernel<<<tb_blocks, 256, 0, ctx->stream>>>(hf, x, y, hd, depth, 1, 0);
+        TL_CHECK_LAUNCH(ctx);
+      }
+    }
+  }
+  return TL_OK;
+}
+
+__global__ void pack_kernel(int x, int y, int hd, int depth, int face, int pack,
+                            double* field, double* buffer) {
+  /* TeaLeaf/c_kernels/sycl/pack_halos.cpp:7-184 */
+  const bool lr = (face == TL_CHUNK_LEFT || face == TL_CHUNK_RIGHT);
+  const long n = lr ? (long)y * depth : (long)x * depth;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n;
+       t += (long)gridDim.x * blockDim.x) {
+    long fi;
+    if (lr) {
+      const int jj = (int)(t / depth), d = (int)(t % depth);
+      int col;
+      if (face == TL_CHUNK_LEFT) col = pack ? hd : hd - depth;
+      else col = pack ? x - hd - depth : x - hd;
+      fi = (long)jj * x + col + d;
+    } else {
+      int row;
+      if (face == TL_CHUNK_BOTTOM) row = pack ? hd : hd - depth;
+      else row = pack ? y - hd - depth : y - hd;
+      fi = (long)row * x + t;
+    }
+    if (pack) buffer[t] = field[fi];
+    else field[fi] = buffer[t];
+  }
+}
+
+/* -------------------------------------------------- persistent CG solve */
+
+struct CgPersistParams {
+  int x, y, hd, ntiles, max_iters;
+  double eps, rro;
+  double *u, *p, *r, *w;
+  const double *kx, *ky;
+  double *part_w, *part_r;
+  double *pw_hist, *rrn_hist;
+  unsigned* sync;
+  int* status;
+  int* steps_out;
+};
+
+/* One CG step loop of TeaLeaf/drivers/cg_driver.c:18-25 with the kernels of
+ * TeaLeaf/c_kernels/sycl/cg.cpp:137-281, all on the device. Each block owns
+ * tiles blockIdx.x, blockIdx.x + gridDim.x, ... in every phase. The p halo
+ * cells that the stencil reads (depth 1 on each face) are written by the
+ * owner of the adjacent interior cell in the p update, which yields the
+ * same values as the reference's halo update; corner and outer halo cells
+ * are brought up to date by the exact halo update launched after the loop. */
+__global__ void __launch_bounds__(kPersistThreads, 1)
+cg_persistent_kernel(CgPersistParams P) {
+  __shared__ double s_group[TL_GROUP];
+  __shared__ double s_scratch[TL_RED_SCRATCH];
+  const int x = P.x, y = P.y, hd = P.hd;
+  const unsigned len = (unsigned)x * (unsigned)y;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const double* __restrict__ kx = P.kx;
+  const double* __restrict__ ky = P.ky;
+  double rro = P.rro;
+  int steps = 0;
+
+  for (int k = 0; k < P.max_iters; ++k) {
+    /* ---- w = A p, pw partials (cg_calc_w) */
+    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+      const unsigned base = (unsigned)tile * TL_TILE;
+      for (int g = warp; g < TL_GROUP; g += nwarps) {
+        const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
+        double c0 = 0.0, c1 = 0.0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const unsigned i = i0 + h;
+          if (i < len) {
+            const int jj = (int)(i / (unsigned)x);
+            const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+            if (interior(kk, jj, x, y, hd)) {
+              const double s = smvp(L2Load{P.p}, kx, ky, i, x);
+              P.w[i] = s;
+              const double c = s * __ldcg(P.p + i);
+              if (h == 0) c0 = c; else c1 = c;
+            }
+          }
+        }
+        const double v = tl_tree64(c0, c1);
+        if (lane == 0) s_group[g] = v;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        const double v = tl_tree64(s_group[2 * lane], s_group[2 * lane + 1]);
+        if (lane == 0) P.part_w[tile] = v;
+      }
+      __syncthreads();
+    }
+    if (!tl_grid_barrier(P.sync, P.status)) break;
+    const double pw = tl_reduce_partials(P.part_w, P.ntiles, s_scratch);
+    const double alpha = rro / pw;
+
+    /* ---- u += alpha p, r -= alpha w, rrn partials (cg_calc_ur) */
+    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+      const unsigned base = (unsigned)tile * TL_TILE;
+      for (int g = warp; g < TL_GROUP; g += nwarps) {
+        const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
+        double c0 = 0.0, c1 = 0.0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const unsigned i = i0 + h;
+          if (i < len) {
+            const int jj = (int)(i / (unsigned)x);
+            const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+            if (interior(kk, jj, x, y, hd)) {
+              P.u[i] = __ldcg(P.u + i) + alpha * __ldcg(P.p + i);
+              const double rv = __ldcg(P.r + i) - alpha * __ldcg(P.w + i);
+              P.r[i] = rv;
+              const double c = rv * rv;
+              if (h == 0) c0 = c; else c1 = c;
+            }
+          }
+        }
+        const double v = tl_tree64(c0, c1);
+        if (lane == 0) s_group[g] = v;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        const double v = tl_tree64(s_group[2 * lane], s_group[2 * lane + 1]);
+        if (lane == 0) P.part_r[tile] = v;
+      }
+      __syncthreads();
+    }
+    if (!tl_grid_barrier(P.sync, P.status)) break;
+    const double rrn = tl_reduce_partials(P.part_r, P.ntiles, s_scratch);
+    const double beta = rrn / rro;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      P.pw_hist[k] = pw;
+      P.rrn_hist[k] = rrn;
+    }
+
+    /* ---- p = beta p + r (cg_calc_p), plus the depth-1 face halos of p */
+    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+      const unsigned base = (unsigned)tile * TL_TILE;
+      for (unsigned t = threadIdx.x; t < TL_TILE; t += blockDim.x) {
+        const unsigned i = base + t;
+        if (i >= len) break;
+        const int jj = (int)(i / (unsigned)x);
+        const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+        if (!interior(kk, jj, x, y, hd)) continue;
+        const double pv = beta * __ldcg(P.p + i) + __ldcg(P.r + i);
+        P.p[i] = pv;
+        if (kk == hd) P.p[i - 1] = pv;
+        if (kk == x - hd - 1) P.p[i + 1] = pv;
+        if (jj == hd) P.p[i - x] = pv;
+        if (jj == y - hd - 1) P.p[i + x] = pv;
+      }
+    }
+    rro = rrn;
+    steps = k + 1;
+    if (sqrt(fabs(rrn)) < P.eps) break;
+    if (!tl_grid_barrier(P.sync, P.status)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.steps_out = steps;
+}
+
+}  // namespace
+
+/* ================================================================ ABI */
+
+#define CTX_OK(ctx) TL_REQUIRE((ctx) != nullptr, "null context")
+#define DIMS_OK(x, y, hd) \
+  TL_REQUIRE((x) > 2 * (hd) && (y) > 2 * (hd) && (hd) >= 1, "invalid grid dimensions")
+
+extern "C" int tl_set_chunk_data_vertices(tl_context* ctx, int x, int y, int hd,
+                                          double* vertex_x, double* vertex_y,
+                                          double x_min, double y_min, double dx,
+                                          double dy) {
+  CTX_OK(ctx);
+  TL_REQUIRE(vertex_x && vertex_y, "null vertex array");
+  const int n = (x > y ? x : y) + 1;
+  vertices_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(x, y, hd, vertex_x, vertex_y,
+                                                             x_min, y_min, dx, dy);
+  TL_CHECK_LAUNCH(ctx);
+  return TL_OK;
+}
+
+extern "C" int tl_set_chunk_data(tl_context* ctx, int x, int y, int hd,
+                                 const double* vertex_x, const double* vertex_y,
+                                 double* cell_x, double* cell_y, double* volume,
+                                 double* x_area, double* y_area, double x_min,
+                                 double y_min, double dx, double dy) {
+  CTX_OK(ctx);
+  (void)hd; (void)x_min; (void)y_min;
+  return launch_map(ctx, ChunkDataOp{x, y, vertex_x, vertex_y, cell_x, cell_y, volume,
+                                     x_area, y_area, dx, dy},
+                    x, y);
+}
+
+extern "C" int tl_set_chunk_initial_state(tl_context* ctx, int x, int y,
+                                          double default_energy,
+                                          double default_density, double* energy0,
+                                          double* density) {
+  CTX_OK(ctx);
+  return launch_map(ctx, InitialStateOp{default_energy, default_density, energy0, density},
+                    x, y);
+}
+
+extern "C" int tl_set_chunk_state(tl_context* ctx, int x, int y, int hd,
+                                  const tl_state* state, double* energy0,
+                                  double* density, double* u, const double* cell_x,
+                                  const double* cell_y, const double* vertex_x,
+                                  const double* vertex_y) {
+  CTX_OK(ctx);
+  (void)hd;
+  TL_REQUIRE(state != nullptr, "null state");
+  return launch_map(ctx, StateOp{x, y, *state, energy0, density, u, cell_x, cell_y,
+                                 vertex_x, vertex_y},
+                    x, y);
+}
+
+extern "C" int tl_store_energy(tl_context* ctx, int x, int y, double* energy,
+                               const double* energy0) {
+  CTX_OK(ctx);
+  return launch_map(ctx, CopyAllOp{energy, energy0}, x, y);
+}
+
+extern "C" int tl_update_face(tl_context* ctx, int x, int y, int hd,
+                              double* field, int face, int depth) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(face >= 0 && face < 4, "invalid face");
+  double* fields[1] = {field};
+  return launch_halos(ctx, x, y, hd, depth, 1 << face, fields, 1);
+}
+
+extern "C" int tl_local_halos(tl_context* ctx, int x, int y, int hd, int depth,
+                              int face_mask, double* const* fields, int nfields) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(nfields == 0 || fields != nullptr, "null field list");
+  return launch_halos(ctx, x, y, hd, depth, face_mask, fields, nfields);
+}
+
+extern "C" int tl_pack_or_unpack(tl_context* ctx, int x, int y, int hd, int depth,
+                                 int face, int pack, double* field, double* buffer) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(field && buffer, "null field or buffer");
+  TL_REQUIRE(face >= 0 && face < 4 && depth >= 1 && depth <= hd, "invalid face or depth");
+  const size_t n = (face == TL_CHUNK_LEFT || face == TL_CHUNK_RIGHT) ? (size_t)y * depth
+                                                                      : (size_t)x * depth;
+  int rc = tl_ensure_stage(ctx, n);
+  if (rc != TL_OK) return rc;
+  if (!pack) {
+    TL_CUDA(cudaMemcpyAsync(ctx->d_stage, buffer, n * sizeof(double),
+                            cudaMemcpyHostToDevice, ctx->stream));
+  }
+  pack_kernel<<<(int)std::min<size_t>((n + 255) / 256, 1024), 256, 0, ctx->stream>>>(
+      x, y, hd, depth, face, pack, field, ctx->d_stage);
+  TL_CHECK_LAUNCH(ctx);
+  if (pack) {
+    TL_CUDA(cudaMemcpyAsync(buffer, ctx->d_stage, n * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  return TL_OK;
+}
+
+extern "C" int tl_field_summary(tl_context* ctx, int x, int y, int hd,
+                                const double* u, const double* density,
+                                const double* energy0, const double* volume,
+                                double* vol, double* mass, double* ie, double* temp) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(vol && mass && ie && temp, "null summary output");
+  double out[4];
+  int rc = launch_reduce(ctx, SummaryOp{u, density, energy0, volume}, x, y, hd, out);
+  if (rc != TL_OK) return rc;
+  *vol = out[0];
+  *mass = out[1];
+  *ie = out[2];
+  *temp = out[3];
+  return TL_OK;
+}
+
+static int cg_init_impl(tl_context* ctx, int x, int y, int hd, int coefficient,
+                        double rx, double ry, double* p, double* r, double* u,
+                        double* w, double* kx, double* ky, const double* density,
+                        const double* energy, double* rro_sum) {
+  int rc = launch_map(ctx, CgInitUOp{coefficient, p, r, u, w, density, energy, x, y}, x, y);
+  if (rc != TL_OK) return rc;
+  rc = launch_map(ctx, CgInitKOp{x, y, hd, w, kx, ky, rx, ry}, x, y);
+  if (rc != TL_OK) return rc;
+  return launch_reduce(ctx, CgInitOthersOp{x, kx, ky, u, p, r, w}, x, y, hd, rro_sum);
+}
+
+extern "C" int tl_cg_init(tl_context* ctx, int x, int y, int hd, int coefficient,
+                          double rx, double ry, double* p, double* r, double* u,
+                          double* w, double* kx, double* ky, const double* density,
+                          const double* energy, double* rro) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(rro != nullptr, "null rro");
+  double s = 0.0;
+  int rc = cg_init_impl(ctx, x, y, hd, coefficient, rx, ry, p, r, u, w, kx, ky, density,
+                        energy, &s);
+  if (rc != TL_OK) return rc;
+  *rro += s;
+  return TL_OK;
+}
+
+extern "C" int tl_cg_calc_w(tl_context* ctx, int x, int y, int hd, double* w,
+                            const double* p, const double* kx, const double* ky,
+                            double* pw) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(pw != nullptr, "null pw");
+  double s = 0.0;
+  int rc = launch_reduce(ctx, CgCalcWOp{x, p, kx, ky, w}, x, y, hd, &s);
+  if (rc != TL_OK) return rc;
+  *pw += s;
+  return TL_OK;
+}
+
+extern "C" int tl_cg_calc_ur(tl_context* ctx, int x, int y, int hd, double* u,
+                             double* r, const double* p, const double* w,
+                             double alpha, double* rrn) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(rrn != nullptr, "null rrn");
+  double s = 0.0;
+  int rc = launch_reduce(ctx, CgCalcUrOp{u, r, p, w, alpha}, x, y, hd, &s);
+  if (rc != TL_OK) return rc;
+  *rrn = s;
+  return TL_OK;
+}
+
+extern "C" int tl_cg_calc_p(tl_context* ctx, int x, int y, int hd, double beta,
+                            double* p, const double* r) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, CgCalcPOp{x, y, hd, beta, p, r}, x, y);
+}
+
+extern "C" int tl_copy_u(tl_context* ctx, int x, int y, int hd, const double* u,
+                         double* u0) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
+}
+
+extern "C" int tl_calculate_residual(tl_context* ctx, int x, int y, int hd,
+                                     const double* u, const double* u0, double* r,
+                                     const double* kx, const double* ky) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, ResidualOp{x, y, hd, u, u0, kx, ky, r}, x, y);
+}
+
+extern "C" int tl_calculate_2norm(tl_context* ctx, int x, int y, int hd,
+                                  const double* buffer, double* norm) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(norm != nullptr, "null norm");
+  double s = 0.0;
+  int rc = launch_reduce(ctx, Norm2Op{buffer}, x, y, hd, &s);
+  if (rc != TL_OK) return rc;
+  *norm = s;
+  return TL_OK;
+}
+
+extern "C" int tl_finalise(tl_context* ctx, int x, int y, int hd, const double* u,
+                           const double* density, double* energy) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, FinaliseOp{x, y, hd, u, density, energy}, x, y);
+}
+
+extern "C" int tl_jacobi_init(tl_context* ctx, int x, int y, int hd, int coefficient,
+                              double rx, double ry, double* u, double* u0,
+                              const double* density, const double* energy, double* kx,
+                              double* ky) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, JacobiInitOp{x, y, hd, coefficient, rx, ry, u, u0, kx, ky,
+                                      density, energy},
+                    x, y);
+}
+
+extern "C" int tl_jacobi_iterate(tl_context* ctx, int x, int y, int hd, double* u,
+                                 const double* u0, double* r, const double* kx,
+                                 const double* ky, double* error) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(error != nullptr, "null error");
+  int rc = launch_map(ctx, CopyAllOp{r, u}, x, y);
+  if (rc != TL_OK) return rc;
+  double s = 0.0;
+  rc = launch_reduce(ctx, JacobiIterateOp{x, u, u0, r, kx, ky}, x, y, hd, &s);
+  if (rc != TL_OK) return rc;
+  *error = s;
+  return TL_OK;
+}
+
+extern "C" int tl_cheby_init(tl_context* ctx, int x, int y, int hd, double theta,
+                             double* p, double* r, const double* u, const double* u0,
+                             double* w, const double* kx, const double* ky) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, ChebyInitOp{x, y, hd, theta, p, r, w, u, u0, kx, ky}, x, y);
+}
+
+extern "C" int tl_cheby_iterate(tl_context* ctx, int x, int y, int hd, double alpha,
+                                double beta, double* p, double* r, double* u,
+                                const double* u0, double* w, const double* kx,
+                                const double* ky) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  int rc = launch_map(ctx, ChebyIterateOp{x, y, hd, alpha, beta, p, r, w, u, u0, kx, ky},
+                      x, y);
+  if (rc != TL_OK) return rc;
+  return launch_map(ctx, AddInteriorOp{x, y, hd, p, u}, x, y);
+}
+
+extern "C" int tl_ppcg_init(tl_context* ctx, int x, int y, int hd, double theta,
+                            double* sd, const double* r) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  return launch_map(ctx, PpcgInitOp{x, y, hd, theta, sd, r}, x, y);
+}
+
+extern "C" int tl_ppcg_inner_iteration(tl_context* ctx, int x, int y, int hd,
+                                       double theta, double alpha, double beta,
+                                       double* sd, double* r, double* u,
+                                       const double* kx, const double* ky) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  (void)theta;
+  int rc = launch_map(ctx, PpcgCalcUrOp{x, y, hd, sd, kx, ky, r, u}, x, y);
+  if (rc != TL_OK) return rc;
+  return launch_map(ctx, PpcgCalcSdOp{x, y, hd, alpha, beta, sd, r}, x, y);
+}
+
+extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficient,
+                           double rx, double ry, double eps, int max_iters, double* p,
+                           double* r, double* u, double* u0, double* w, double* kx,
+                           double* ky, const double* density, const double* energy,
+                           double* rro0, double* pw_hist, double* rrn_hist, int* steps) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(rro0 && steps && (max_iters == 0 || (pw_hist && rrn_hist)),
+             "null output of tl_cg_solve");
+  TL_REQUIRE(max_iters >= 0, "negative max_iters");
+  *steps = 0;
+
+  /* cg_init_driver: init kernels, halo of u and p, u0 = u. */
+  double rro = 0.0;
+  int rc = cg_init_impl(ctx, x, y, hd, coefficient, rx, ry, p, r, u, w, kx, ky, density,
+                        energy, &rro);
+  if (rc != TL_OK) return rc;
+  *rro0 += rro;
+  double* up[2] = {u, p};
+  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
+  if (rc != TL_OK) return rc;
+  rc = launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
+  if (rc != TL_OK) return rc;
+  if (max_iters == 0) return TL_OK;
+
+  const size_t ntiles = tl_num_tiles(x, y);
+  rc = tl_ensure_partials(ctx, ntiles);
+  if (rc != TL_OK) return rc;
+  rc = tl_ensure_history(ctx, (size_t)max_iters);
+  if (rc != TL_OK) return rc;
+
+  int per_sm = 0;
+  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_persistent_kernel,
+                                                        kPersistThreads, 0));
+  TL_REQUIRE(per_sm >= 1, "persistent CG kernel cannot be resident");
+  int grid = ctx->num_sms * std::min(per_sm, 1);
+  if ((size_t)grid > ntiles) grid = (int)ntiles;
+
+  CgPersistParams P;
+  P.x = x; P.y = y; P.hd = hd; P.ntiles = (int)ntiles; P.max_iters = max_iters;
+  P.eps = eps; P.rro = rro;
+  P.u = u; P.p = p; P.r = r; P.w = w; P.kx = kx; P.ky = ky;
+  P.part_w = ctx->d_part; P.part_r = ctx->d_part + ctx->part_cap;
+  P.pw_hist = ctx->d_hist; P.rrn_hist = ctx->d_hist + ctx->hist_cap;
+  P.sync = ctx->d_sync; P.status = ctx->d_status; P.steps_out = ctx->d_steps;
+  TL_CUDA(cudaMemsetAsync(ctx->d_sync + TL_SYNC_BAR_COUNT, 0, 2 * sizeof(unsigned),
+                          ctx->stream));
+  TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  ctx->h_steps[0] = -1;
+  void* args[] = {&P};
+  TL_CUDA(cudaLaunchCooperativeKernel((const void*)cg_persistent_kernel, dim3(grid),
+                                      dim3(kPersistThreads), args, 0, ctx->stream));
+  TL_CHECK_LAUNCH(ctx);
+  /* Final state of the u and p halos, as after the reference's last halo
+   * update of the loop. */
+  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
+  if (rc != TL_OK) return rc;
+  int status = 0;
+  TL_CUDA(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (status != 0) {
+    return tl_set_error(status, "persistent CG kernel reported a grid-barrier timeout");
+  }
+  const int n = ((volatile int*)ctx->h_steps)[0];
+  TL_REQUIRE(n >= 0 && n <= max_iters, "persistent CG kernel did not report its steps");
+  if (n > 0) {
+    TL_CUDA(cudaMemcpyAsync(pw_hist, ctx->d_hist, (size_t)n * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    TL_CUDA(cudaMemcpyAsync(rrn_hist, ctx->d_hist + ctx->hist_cap, (size_t)n * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  *steps = n;
+  return TL_OK;
+}

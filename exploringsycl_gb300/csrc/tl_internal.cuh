@@ -1,0 +1,205 @@
+/*
+ * tl_internal.cuh -- shared internals of the GB300 TeaLeaf backend:
+ * the context, error reporting, the deterministic reduction primitives and
+ * the bounded grid barrier of the persistent kernels.
+ *
+ * Reduction order. Every dot product is summed exactly as the reference
+ * sums it: values of 64 consecutive linear cells (halo cells contribute 0)
+ * are combined by a pairwise tree whose stride doubles from 1 to 32
+ * (TeaLeaf/c_kernels/sycl/cg.cpp:113-126), and the resulting partial sums
+ * are reduced level by level by the same 64-wide tree, padded with zeros
+ * (TeaLeaf/c_kernels/sycl/sycl_shared.hpp:35-79).
+ *
+ * On the GPU a warp holds one 64-cell group, two consecutive cells per lane:
+ * the in-lane add is the stride-1 level, and a butterfly of shuffles with
+ * lane masks 1, 2, 4, 8, 16 performs the stride-2..32 levels (IEEE addition
+ * is commutative, so both partners of each butterfly step compute the same
+ * bits). A thread block processes "tiles" of 64 groups = 4096 consecutive
+ * cells and folds the 64 group sums of a tile with the same warp tree, giving
+ * one second-level partial per tile. Whatever reduces those tile partials
+ * (the last block of a step-wise kernel, or every block of a persistent
+ * kernel after its grid barrier) continues the tree level by level.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "tealeaf_gb300.h"
+
+#define TL_GROUP 64                       /* cells per first-level group */
+#define TL_TILE (TL_GROUP * TL_GROUP)     /* cells per tile (4096) */
+#define TL_MAX_TILES (1 << 17)            /* grids up to 5.4e8 cells */
+/* Shared scratch of a block-wide reduction of up to TL_MAX_TILES partials:
+ * the first level (TL_MAX_TILES/64 values), then the smaller levels. */
+#define TL_RED_SCRATCH (TL_MAX_TILES / TL_GROUP + TL_MAX_TILES / TL_TILE + 64)
+#define TL_FULL_MASK 0xffffffffu
+
+/* Result slots in the pinned result page. */
+#define TL_SLOT_A 0
+#define TL_SLOT_B 1
+#define TL_SLOT_C 2
+#define TL_SLOT_D 3
+#define TL_NUM_SLOTS 8
+
+/* Sync words in device scratch. */
+#define TL_SYNC_TICKET 0     /* last-block tickets, one per slot group */
+#define TL_SYNC_BAR_COUNT 8  /* grid barrier arrival counter */
+#define TL_SYNC_BAR_GEN 9    /* grid barrier generation */
+#define TL_SYNC_WORDS 16
+
+/* How long a block waits at a grid barrier before it gives up and reports
+ * TL_ERR_TIMEOUT (nanoseconds of %globaltimer). */
+#define TL_BARRIER_BUDGET_NS 2000000000ull
+
+struct tl_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+
+  double* d_part = nullptr;       /* 4 tile-partial arrays of part_cap doubles */
+  size_t part_cap = 0;
+  unsigned* d_sync = nullptr;     /* TL_SYNC_WORDS words */
+  int* d_status = nullptr;        /* kernel-reported error code */
+  double* h_result = nullptr;     /* pinned, mapped: TL_NUM_SLOTS doubles */
+  double* d_result = nullptr;     /* device alias of h_result */
+  int* h_steps = nullptr;         /* pinned, mapped: persistent-solve counters */
+  int* d_steps = nullptr;
+  double* d_hist = nullptr;       /* 2 x hist_cap doubles of per-step scalars */
+  size_t hist_cap = 0;
+  double* d_stage = nullptr;      /* halo pack staging */
+  size_t stage_cap = 0;
+  long long launches = 0;
+};
+
+/* Thread-local error message and helpers (tl_context.cu). */
+int tl_set_error(int code, const std::string& msg);
+int tl_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+int tl_ensure_partials(tl_context* ctx, size_t ntiles);
+int tl_ensure_history(tl_context* ctx, size_t n);
+int tl_ensure_stage(tl_context* ctx, size_t n);
+
+#define TL_CUDA(call)                                                      \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) return tl_cuda_error(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define TL_CHECK_LAUNCH(ctx)                                               \
+  do {                                                                     \
+    (ctx)->launches++;                                                     \
+    cudaError_t e_ = cudaGetLastError();                                   \
+    if (e_ != cudaSuccess) return tl_cuda_error(e_, "kernel launch", __FILE__, __LINE__); \
+  } while (0)
+
+#define TL_REQUIRE(cond, msg)                                              \
+  do {                                                                     \
+    if (!(cond)) return tl_set_error(TL_ERR_ARG, msg);                     \
+  } while (0)
+
+static inline size_t tl_num_tiles(int x, int y) {
+  return ((size_t)x * (size_t)y + TL_TILE - 1) / TL_TILE;
+}
+
+/* ----------------------------------------------------------- device side */
+
+/* Pairwise 64-wide tree over two values per lane (cells 2*lane, 2*lane+1
+ * of the group); every lane returns the group sum. */
+__device__ __forceinline__ double tl_tree64(double a, double b) {
+  double v = a + b;
+  v = v + __shfl_xor_sync(TL_FULL_MASK, v, 1);
+  v = v + __shfl_xor_sync(TL_FULL_MASK, v, 2);
+  v = v + __shfl_xor_sync(TL_FULL_MASK, v, 4);
+  v = v + __shfl_xor_sync(TL_FULL_MASK, v, 8);
+  v = v + __shfl_xor_sync(TL_FULL_MASK, v, 16);
+  return v;
+}
+
+/* Reduces n tile partials (global memory, written by other blocks before a
+ * grid-wide synchronisation) to one value in the reference order, using the
+ * whole block. `scratch` is shared memory of TL_RED_SCRATCH doubles; the
+ * first level goes to scratch[0, ceil(n/64)) and later levels alternate
+ * with the region after it, which each smaller level fits. Every thread
+ * returns the same value. */
+__device__ __forceinline__ double tl_reduce_partials(const double* part, int n,
+                                                     double* scratch) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  int ng = (n + TL_GROUP - 1) / TL_GROUP;
+  double* src = scratch;
+  double* dst = scratch + ng;
+  for (int g = warp; g < ng; g += nwarps) {
+    const int i0 = g * TL_GROUP + 2 * lane;
+    const double a = (i0 < n) ? __ldcg(part + i0) : 0.0;
+    const double b = (i0 + 1 < n) ? __ldcg(part + i0 + 1) : 0.0;
+    const double s = tl_tree64(a, b);
+    if (lane == 0) src[g] = s;
+  }
+  __syncthreads();
+  n = ng;
+  while (n > 1) {
+    ng = (n + TL_GROUP - 1) / TL_GROUP;
+    for (int g = warp; g < ng; g += nwarps) {
+      const int i0 = g * TL_GROUP + 2 * lane;
+      const double a = (i0 < n) ? src[i0] : 0.0;
+      const double b = (i0 + 1 < n) ? src[i0 + 1] : 0.0;
+      const double s = tl_tree64(a, b);
+      if (lane == 0) dst[g] = s;
+    }
+    __syncthreads();
+    double* t = src;
+    src = dst;
+    dst = t;
+    n = ng;
+  }
+  const double total = src[0];
+  __syncthreads();
+  return total;
+}
+
+__device__ __forceinline__ unsigned long long tl_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+/* Grid-wide barrier for co-resident blocks (cooperative launch). Spins for
+ * at most TL_BARRIER_BUDGET_NS; on expiry it records TL_ERR_TIMEOUT in
+ * *status and returns false instead of waiting further. Returns false as
+ * well when any block has recorded an error, so that all blocks leave their
+ * loops together. */
+__device__ __forceinline__ bool tl_grid_barrier(unsigned* sync, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = sync + TL_SYNC_BAR_GEN;
+    const unsigned my_gen = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(sync + TL_SYNC_BAR_COUNT, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(sync + TL_SYNC_BAR_COUNT, 0u);
+      __threadfence();
+      atomicAdd(sync + TL_SYNC_BAR_GEN, 1u);
+    } else {
+      const unsigned long long t0 = tl_globaltimer();
+      while (*gen == my_gen) {
+        if (tl_globaltimer() - t0 > TL_BARRIER_BUDGET_NS) {
+          atomicCAS(status, 0, TL_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)status != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}

@@ -1,0 +1,245 @@
+/*
+ * tealeaf_gb300.h -- C ABI of the GB300 TeaLeaf kernel backend.
+ *
+ * Plain C: device pointers, sizes and host scalars, no C++ or framework types.
+ * The kernel entry points mirror, one for one, the kernel functions that the
+ * reference's SYCL backend calls from its run_* layer
+ * (TeaLeaf/c_kernels/sycl/c_kernels.hpp:1-217, dispatched from
+ * TeaLeaf/c_kernels/sycl/kernel_interface.cpp:34-371); each declaration
+ * names the reference function it replaces. A TeaLeaf maintainer binds them
+ * from a C++ run_* layer (exploringsycl_gb300/backend/kernel_interface.cpp).
+ *
+ * Conventions
+ *  - Fields are device arrays of doubles in the reference layout: row-major,
+ *    index kk + jj*x, x = x_cells + 2*halo_depth, y = y_cells + 2*halo_depth,
+ *    interior kk in [halo_depth, x-halo_depth), jj in [halo_depth, y-halo_depth).
+ *    Allocate them with tl_field_alloc (256-byte aligned, zero-filled).
+ *  - Every call is issued on the context's stream. Calls that return a
+ *    scalar through a host pointer synchronise that stream before returning;
+ *    the others return as soon as the work is queued.
+ *  - Scalars follow the reference: rro and pw are accumulated (+=), while
+ *    rrn, norm, error and the field summary are overwritten
+ *    (TeaLeaf/c_kernels/sycl/cg.cpp:133,194,253; solver_methods.cpp:116;
+ *    jacobi.cpp:241; field_summary.cpp:394-397).
+ *  - Reductions are deterministic and follow the reference's summation
+ *    order exactly (64-wide pairwise trees over consecutive linear cells,
+ *    then over partial sums: TeaLeaf/c_kernels/sycl/cg.cpp:113-126,
+ *    sycl_shared.hpp:35-79), and the double-precision kernels round every
+ *    product and sum separately, so results are bit-identical to a
+ *    sequential evaluation of the reference's expressions.
+ *  - Return value: TL_OK or an error code; tl_last_error() describes the
+ *    most recent failure on the calling thread.
+ */
+#ifndef TEALEAF_GB300_H
+#define TEALEAF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TL_OK 0
+#define TL_ERR_CUDA 1      /* a CUDA call failed (message has details) */
+#define TL_ERR_ARG 2       /* invalid argument (null pointer, bad size) */
+#define TL_ERR_TIMEOUT 3   /* a bounded in-kernel wait gave up */
+#define TL_ERR_STATE 4     /* call out of sequence */
+#define TL_ERR_NUMERIC 5   /* non-finite value or breakdown in a solver */
+
+/* Geometry codes of a state (TeaLeaf/settings.h:130-135). */
+#define TL_RECTANGULAR 0
+#define TL_CIRCULAR 1
+#define TL_POINT 2
+
+/* Faces (TeaLeaf/shared.h:34-37). */
+#define TL_CHUNK_LEFT 0
+#define TL_CHUNK_RIGHT 1
+#define TL_CHUNK_BOTTOM 2
+#define TL_CHUNK_TOP 3
+
+/* Coefficient kinds (TeaLeaf/shared.h:47-48). */
+#define TL_CONDUCTIVITY 1
+#define TL_RECIP_CONDUCTIVITY 2
+
+typedef struct tl_context tl_context;
+
+/* One initial state of the deck (TeaLeaf/settings.h:137-145). */
+typedef struct tl_state {
+  double density;
+  double energy;
+  double x_min;
+  double y_min;
+  double x_max;
+  double y_max;
+  double radius;
+  int geometry;
+} tl_state;
+
+/* ------------------------------------------------------------ context
+ * Replaces the SYCL queue the reference creates in kernel_initialise
+ * (TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:47) and the temporary
+ * reduction buffers each reducing kernel allocates
+ * (TeaLeaf/c_kernels/sycl/cg.cpp:80,145,206): a context owns a CUDA stream
+ * (or borrows the caller's), reduction scratch, pinned result slots and an
+ * error flag. `stream` may be NULL (the context creates its own). */
+int tl_context_create(int device, void* stream, tl_context** out);
+int tl_context_destroy(tl_context* ctx);
+int tl_context_stream(tl_context* ctx, void** stream);
+int tl_synchronize(tl_context* ctx);
+const char* tl_last_error(void);
+/* Number of this library's kernel launches issued on the context so far. */
+long long tl_launch_count(tl_context* ctx);
+
+/* -------------------------------------------------------------- fields
+ * Replace the SYCL buffers of kernel_initialise / kernel_finalise
+ * (TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:31-125). */
+int tl_field_alloc(tl_context* ctx, size_t count, double** dev_out);
+int tl_field_free(tl_context* ctx, double* dev);
+int tl_copy_to_device(tl_context* ctx, double* dev, const double* host,
+                      size_t count);
+int tl_copy_to_host(tl_context* ctx, double* host, const double* dev,
+                    size_t count);
+
+/* ---------------------------------------------------- initialisation */
+/* set_chunk_data_vertices, TeaLeaf/c_kernels/sycl/set_chunk_data.cpp:8-28 */
+int tl_set_chunk_data_vertices(tl_context* ctx, int x, int y, int halo_depth,
+                               double* vertex_x, double* vertex_y,
+                               double x_min, double y_min, double dx,
+                               double dy);
+/* set_chunk_data, TeaLeaf/c_kernels/sycl/set_chunk_data.cpp:31-64 */
+int tl_set_chunk_data(tl_context* ctx, int x, int y, int halo_depth,
+                      const double* vertex_x, const double* vertex_y,
+                      double* cell_x, double* cell_y, double* volume,
+                      double* x_area, double* y_area, double x_min,
+                      double y_min, double dx, double dy);
+/* set_chunk_initial_state, TeaLeaf/c_kernels/sycl/set_chunk_state.cpp:8-27 */
+int tl_set_chunk_initial_state(tl_context* ctx, int x, int y,
+                               double default_energy, double default_density,
+                               double* energy0, double* density);
+/* set_chunk_state, TeaLeaf/c_kernels/sycl/set_chunk_state.cpp:30-92 */
+int tl_set_chunk_state(tl_context* ctx, int x, int y, int halo_depth,
+                       const tl_state* state, double* energy0,
+                       double* density, double* u, const double* cell_x,
+                       const double* cell_y, const double* vertex_x,
+                       const double* vertex_y);
+/* store_energy, TeaLeaf/c_kernels/sycl/store_energy.cpp:6-24 */
+int tl_store_energy(tl_context* ctx, int x, int y, double* energy,
+                    const double* energy0);
+
+/* ------------------------------------------------------------- halos */
+/* update_left / update_right / update_top / update_bottom,
+ * TeaLeaf/c_kernels/sycl/local_halos.cpp:7-102: reflect `depth` layers of
+ * one face. */
+int tl_update_face(tl_context* ctx, int x, int y, int halo_depth,
+                   double* field, int face, int depth);
+/* The whole of run_local_halos (TeaLeaf/c_kernels/sycl/kernel_interface.cpp:
+ * 100-127) for `nfields` fields in one pass per face pair: faces whose bit
+ * (1 << face) is set in face_mask are updated in the order L, R, T, B. */
+int tl_local_halos(tl_context* ctx, int x, int y, int halo_depth, int depth,
+                   int face_mask, double* const* fields, int nfields);
+/* pack_* / unpack_*, TeaLeaf/c_kernels/sycl/pack_halos.cpp:7-184 together
+ * with the host mirror copies of kernel_interface.cpp:129-167; `buffer` is
+ * host memory of y*depth (left/right) or x*depth (top/bottom) doubles. */
+int tl_pack_or_unpack(tl_context* ctx, int x, int y, int halo_depth,
+                      int depth, int face, int pack, double* field,
+                      double* buffer);
+
+/* ----------------------------------------------------- field summary */
+/* field_summary_func, TeaLeaf/c_kernels/sycl/field_summary.cpp:6-151 */
+int tl_field_summary(tl_context* ctx, int x, int y, int halo_depth,
+                     const double* u, const double* density,
+                     const double* energy0, const double* volume,
+                     double* vol, double* mass, double* ie, double* temp);
+
+/* ---------------------------------------------------------------- CG */
+/* cg_init_u + cg_init_k + cg_init_others,
+ * TeaLeaf/c_kernels/sycl/cg.cpp:7-134 (as run_cg_init,
+ * kernel_interface.cpp:192-210); rro += r.p */
+int tl_cg_init(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
+               double rx, double ry, double* p, double* r, double* u,
+               double* w, double* kx, double* ky, const double* density,
+               const double* energy, double* rro);
+/* cg_calc_w, TeaLeaf/c_kernels/sycl/cg.cpp:137-195; pw += w.p */
+int tl_cg_calc_w(tl_context* ctx, int x, int y, int halo_depth, double* w,
+                 const double* p, const double* kx, const double* ky,
+                 double* pw);
+/* cg_calc_ur, TeaLeaf/c_kernels/sycl/cg.cpp:198-254; rrn = r.r */
+int tl_cg_calc_ur(tl_context* ctx, int x, int y, int halo_depth, double* u,
+                  double* r, const double* p, const double* w, double alpha,
+                  double* rrn);
+/* cg_calc_p, TeaLeaf/c_kernels/sycl/cg.cpp:257-281 */
+int tl_cg_calc_p(tl_context* ctx, int x, int y, int halo_depth, double beta,
+                 double* p, const double* r);
+
+/* Whole CG solve of one timestep on the device, for the run-ahead mode of
+ * the run_* layer. Equivalent to the reference driver sequence
+ * (TeaLeaf/drivers/cg_driver.c:7-66 with the kernels of cg.cpp):
+ * cg_init (rro), halo update of u and p (depth 1), u0 = u, then up to
+ * max_iters main steps {pw = w.p; alpha = rro/pw; rrn = r.r after the u/r
+ * update; beta = rrn/rro; p = beta p + r; halo of u, p} stopping after the
+ * first step with sqrt(|rrn|) < eps. Runs as one persistent cooperative
+ * kernel with deterministic grid-wide reductions; results and per-step
+ * scalars are bit-identical to the step-wise entry points.
+ * On return: *rro0 += initial r.p; pw_hist[k], rrn_hist[k] (host arrays of
+ * max_iters doubles) hold the scalars of step k; *steps = number of main
+ * steps executed (the driver prints steps-1 when it converged). */
+int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
+                int coefficient, double rx, double ry, double eps,
+                int max_iters, double* p, double* r, double* u, double* u0,
+                double* w, double* kx, double* ky, const double* density,
+                const double* energy, double* rro0, double* pw_hist,
+                double* rrn_hist, int* steps);
+
+/* ------------------------------------------------- solver methods */
+/* copy_u, TeaLeaf/c_kernels/sycl/solver_methods.cpp:7-31 */
+int tl_copy_u(tl_context* ctx, int x, int y, int halo_depth, const double* u,
+              double* u0);
+/* calculate_residual, TeaLeaf/c_kernels/sycl/solver_methods.cpp:34-65 */
+int tl_calculate_residual(tl_context* ctx, int x, int y, int halo_depth,
+                          const double* u, const double* u0, double* r,
+                          const double* kx, const double* ky);
+/* calculate_2norm, TeaLeaf/c_kernels/sycl/solver_methods.cpp:68-117 */
+int tl_calculate_2norm(tl_context* ctx, int x, int y, int halo_depth,
+                       const double* buffer, double* norm);
+/* finalise, TeaLeaf/c_kernels/sycl/solver_methods.cpp:120-145 */
+int tl_finalise(tl_context* ctx, int x, int y, int halo_depth,
+                const double* u, const double* density, double* energy);
+
+/* ------------------------------------------------------------ Jacobi */
+/* jacobi_init, TeaLeaf/c_kernels/sycl/jacobi.cpp:7-56 */
+int tl_jacobi_init(tl_context* ctx, int x, int y, int halo_depth,
+                   int coefficient, double rx, double ry, double* u,
+                   double* u0, const double* density, const double* energy,
+                   double* kx, double* ky);
+/* jacobi_copy_u + jacobi_iterate, TeaLeaf/c_kernels/sycl/jacobi.cpp:59-137
+ * (as run_jacobi_iterate, kernel_interface.cpp:287-300); error = sum|du| */
+int tl_jacobi_iterate(tl_context* ctx, int x, int y, int halo_depth,
+                      double* u, const double* u0, double* r,
+                      const double* kx, const double* ky, double* error);
+
+/* --------------------------------------------------------- Chebyshev */
+/* cheby_init, TeaLeaf/c_kernels/sycl/cheby.cpp:7-38 */
+int tl_cheby_init(tl_context* ctx, int x, int y, int halo_depth, double theta,
+                  double* p, double* r, const double* u, const double* u0,
+                  double* w, const double* kx, const double* ky);
+/* cheby_iterate + cheby_calc_u, TeaLeaf/c_kernels/sycl/cheby.cpp:41-110 */
+int tl_cheby_iterate(tl_context* ctx, int x, int y, int halo_depth,
+                     double alpha, double beta, double* p, double* r,
+                     double* u, const double* u0, double* w,
+                     const double* kx, const double* ky);
+
+/* -------------------------------------------------------------- PPCG */
+/* ppcg_init, TeaLeaf/c_kernels/sycl/ppcg.cpp:7-30 */
+int tl_ppcg_init(tl_context* ctx, int x, int y, int halo_depth, double theta,
+                 double* sd, const double* r);
+/* ppcg_calc_ur + ppcg_calc_sd, TeaLeaf/c_kernels/sycl/ppcg.cpp:33-94 */
+int tl_ppcg_inner_iteration(tl_context* ctx, int x, int y, int halo_depth,
+                            double theta, double alpha, double beta,
+                            double* sd, double* r, double* u,
+                            const double* kx, const double* ky);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TEALEAF_GB300_H */
