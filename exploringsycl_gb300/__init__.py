@@ -32,6 +32,10 @@ class TLError(RuntimeError):
     """A C-ABI call returned an error code."""
 
 
+class TLSolveStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_float), ("steps", C.c_int), ("kernel_launches", C.c_int)]
+
+
 class TLState(C.Structure):
     _fields_ = [("density", C.c_double), ("energy", C.c_double), ("x_min", C.c_double),
                 ("y_min", C.c_double), ("x_max", C.c_double), ("y_max", C.c_double),
@@ -83,6 +87,7 @@ CONTEXT_FREE = {
     "tl_field_free": [_P, _P],
     "tl_copy_to_device": [_P, _P, _P, C.c_size_t],
     "tl_copy_to_host": [_P, _P, _P, C.c_size_t],
+    "tl_last_solve_stats": [_P, C.POINTER(TLSolveStats)],
 }
 
 _lib = None
@@ -164,6 +169,11 @@ class Context:
 
     def synchronize(self) -> None:
         check(self.lib.tl_synchronize(self.h), "tl_synchronize")
+
+    def solve_stats(self) -> TLSolveStats:
+        st = TLSolveStats()
+        check(self.lib.tl_last_solve_stats(self.h, C.byref(st)), "tl_last_solve_stats")
+        return st
 
     def launches(self) -> int:
         return int(self.lib.tl_launch_count(self.h))

@@ -66,6 +66,8 @@ extern "C" int tl_context_create(int device, void* stream, tl_context** out) {
   if (e == cudaSuccess) e = cudaHostGetDevicePointer(&ctx->d_result, ctx->h_result, 0);
   if (e == cudaSuccess) e = cudaHostAlloc(&ctx->h_steps, 8 * sizeof(int), cudaHostAllocMapped);
   if (e == cudaSuccess) e = cudaHostGetDevicePointer(&ctx->d_steps, ctx->h_steps, 0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_stop);
   if (e != cudaSuccess) {
     tl_context_destroy(ctx);
     return tl_cuda_error(e, "context scratch allocation", __FILE__, __LINE__);
@@ -87,6 +89,8 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_stage);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
   if (ctx->h_steps) cudaFreeHost(ctx->h_steps);
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+  if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return TL_OK;
@@ -101,6 +105,12 @@ extern "C" int tl_context_stream(tl_context* ctx, void** stream) {
 extern "C" int tl_synchronize(tl_context* ctx) {
   TL_REQUIRE(ctx, "tl_synchronize: null context");
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  return TL_OK;
+}
+
+extern "C" int tl_last_solve_stats(tl_context* ctx, tl_solve_stats* out) {
+  TL_REQUIRE(ctx && out, "tl_last_solve_stats: null argument");
+  *out = ctx->last_solve;
   return TL_OK;
 }
 

@@ -1067,9 +1067,11 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
   TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   ctx->h_steps[0] = -1;
   void* args[] = {&P};
+  TL_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
   TL_CUDA(cudaLaunchCooperativeKernel((const void*)cg_persistent_kernel, dim3(grid),
                                       dim3(kPersistThreads), args, 0, ctx->stream));
   TL_CHECK_LAUNCH(ctx);
+  TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
   /* Final state of the u and p halos, as after the reference's last halo
    * update of the loop. */
   rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
@@ -1091,5 +1093,10 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
     TL_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   *steps = n;
+  float ms = 0.0f;
+  TL_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  ctx->last_solve.kernel_ms = ms;
+  ctx->last_solve.steps = n;
+  ctx->last_solve.kernel_launches = 1;
   return TL_OK;
 }

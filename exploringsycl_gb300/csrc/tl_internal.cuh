@@ -73,6 +73,9 @@ struct tl_context {
   double* d_stage = nullptr;      /* halo pack staging */
   size_t stage_cap = 0;
   long long launches = 0;
+  cudaEvent_t ev_start = nullptr;  /* around the persistent kernel of a solve */
+  cudaEvent_t ev_stop = nullptr;
+  tl_solve_stats last_solve = {0.0f, 0, 0};
 };
 
 /* Thread-local error message and helpers (tl_context.cu). */

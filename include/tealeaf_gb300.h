@@ -190,6 +190,16 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
                 const double* energy, double* rro0, double* pw_hist,
                 double* rrn_hist, int* steps);
 
+/* Device timing of the most recent solve on this context: the persistent
+ * kernel alone, measured with CUDA events recorded on the context's stream
+ * around its launch, and the number of solver steps it executed. */
+typedef struct tl_solve_stats {
+  float kernel_ms;
+  int steps;
+  int kernel_launches;
+} tl_solve_stats;
+int tl_last_solve_stats(tl_context* ctx, tl_solve_stats* out);
+
 /* ------------------------------------------------- solver methods */
 /* copy_u, TeaLeaf/c_kernels/sycl/solver_methods.cpp:7-31 */
 int tl_copy_u(tl_context* ctx, int x, int y, int halo_depth, const double* u,
