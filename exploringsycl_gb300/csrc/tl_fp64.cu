@@ -21,6 +21,8 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "tl_internal.cuh"
 
@@ -1098,5 +1100,65 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
   ctx->last_solve.kernel_ms = ms;
   ctx->last_solve.steps = n;
   ctx->last_solve.kernel_launches = 1;
+  return TL_OK;
+}
+
+/* ====================================== allocation-free cg_calc_w variant
+ *
+ * tl_cg_calc_w_noalloc computes exactly what tl_cg_calc_w computes (same
+ * kernel, same summation order, same bits) without a context and without
+ * allocating anything: its reduction scratch (one partial per 4096-cell
+ * tile, the final sum and the last-block ticket) lives in the fixed array
+ * below, which every GPU that loads this library holds until the process
+ * exits. Host code may not use the array's name as a device address, so the
+ * address is looked up with cudaGetSymbolAddress, once per device, on the
+ * first call made while that device is current. */
+#define TL_NOALLOC_MAX_TILES 32768 /* 32768 tiles = 134,217,728 cells */
+
+static __device__ __align__(256) double g_noalloc_scratch[TL_NOALLOC_MAX_TILES + 2];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_address[kNoallocMaxDevices] = {};
+}  // namespace
+
+extern "C" int tl_cg_calc_w_noalloc(void* stream, int x, int y, int hd, double* w,
+                                    const double* p, const double* kx, const double* ky,
+                                    double* pw) {
+  TL_REQUIRE(x > 2 * hd && y > 2 * hd && hd >= 1, "invalid grid dimensions");
+  const size_t ntiles = tl_num_tiles(x, y);
+  if (ntiles > TL_NOALLOC_MAX_TILES) {
+    return tl_set_error(TL_ERR_ARG,
+                        "tl_cg_calc_w_noalloc: grid of " + std::to_string((size_t)x * y) +
+                            " cells exceeds the fixed scratch limit of 134217728 cells "
+                            "(32768 tiles of 4096)");
+  }
+  TL_REQUIRE(w && p && kx && ky && pw, "tl_cg_calc_w_noalloc: null argument");
+  int dev = 0;
+  TL_CUDA(cudaGetDevice(&dev));
+  TL_REQUIRE(dev >= 0 && dev < kNoallocMaxDevices, "tl_cg_calc_w_noalloc: device ordinal");
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[dev]) {
+      void* addr = nullptr;
+      TL_CUDA(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
+      g_noalloc_address[dev] = (double*)addr;
+    }
+    scratch = g_noalloc_address[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* result = scratch + TL_NOALLOC_MAX_TILES;
+  unsigned* ticket = (unsigned*)(scratch + TL_NOALLOC_MAX_TILES + 1);
+  TL_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
+  reduce_kernel<CgCalcWOp><<<(unsigned)ntiles, kRedThreads, 0, s>>>(
+      CgCalcWOp{x, p, kx, ky, w}, x, y, hd, scratch, (size_t)TL_NOALLOC_MAX_TILES,
+      (int)ntiles, ticket, result);
+  TL_CUDA(cudaGetLastError());
+  double sum = 0.0;
+  TL_CUDA(cudaMemcpyAsync(&sum, result, sizeof(double), cudaMemcpyDeviceToHost, s));
+  TL_CUDA(cudaStreamSynchronize(s));
+  *pw += sum;
   return TL_OK;
 }

@@ -163,6 +163,27 @@ int tl_cg_init(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
 int tl_cg_calc_w(tl_context* ctx, int x, int y, int halo_depth, double* w,
                  const double* p, const double* kx, const double* ky,
                  double* pw);
+/* Allocation-free variant of tl_cg_calc_w. It has no counterpart in the
+ * reference. It is for callers that must not allocate device memory once
+ * they are running: a TeaLeaf solve embedded in a larger application that
+ * owns the device memory budget, or a caller holding a fixed memory pool,
+ * where a cudaMalloc (which can fail and can synchronise the whole device)
+ * is not allowed mid-run. It takes no context and calls no cudaMalloc,
+ * cudaFree or other allocating routine. Its reduction scratch is a fixed
+ * file-scope device array of 32770 doubles (about 256 KB) that every GPU
+ * loading this library holds until the process exits; grids larger than
+ * 134,217,728 cells (32768 tiles of 4096 cells) are rejected with
+ * TL_ERR_ARG. The first call on a device, with that device current, looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture. Every call shares the array and leaves
+ * its last contents there (the ticket word is cleared at each call): calls
+ * that overlap on the GPU race, so issue them on one stream or serialise
+ * them. `stream` is the caller's cudaStream_t (NULL: the default stream).
+ * Results equal tl_cg_calc_w's bit for bit; pw += w.p, and the call
+ * synchronises `stream` before returning. */
+int tl_cg_calc_w_noalloc(void* stream, int x, int y, int halo_depth, double* w,
+                         const double* p, const double* kx, const double* ky,
+                         double* pw);
 /* cg_calc_ur, TeaLeaf/c_kernels/sycl/cg.cpp:198-254; rrn = r.r */
 int tl_cg_calc_ur(tl_context* ctx, int x, int y, int halo_depth, double* u,
                   double* r, const double* p, const double* w, double alpha,
