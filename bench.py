@@ -218,6 +218,15 @@ def run_reference(args, rank: int, world: int) -> None:
 
 # ----------------------------------------------------------------- GPU side
 
+def max_over_ranks(values: list[float], dist) -> list[float]:
+    """Element-wise maximum over the ranks of a replica job (a no-op alone)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def run_ours(args, rank: int, world: int, dist) -> None:
     import numpy as np
     import torch
@@ -285,11 +294,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         h_energy.copy_(h_out)
     barrier()
 
-    # max over ranks
-    t_local = torch.tensor([total_ms, statistics.mean(e2e_times)], dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
-    total_ms, e2e_mean = float(t_local[0]), float(t_local[1])
+    total_ms, e2e_mean = max_over_ranks([total_ms, statistics.mean(e2e_times)], dist)
 
     if rank != 0:
         ctx.close()

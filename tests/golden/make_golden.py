@@ -1,0 +1,81 @@
+"""Regenerates tests/golden/reference_driver_runs.json.
+
+Runs the reference's own, unchanged TeaLeaf host driver (compiled from the
+reference sources by `make -C oracle ref`, linked with the CPU oracle
+kernels) on a set of decks, and records what it prints: CG step counts,
+per-step error, the full-precision field summaries and the pass/fail check.
+Also records the final field summaries that the reference's Fortran runs
+printed in TeaLeaf/Benchmarks/tea_bm_{1,2,3}.out (line 173 of each).
+
+Needs the reference sources (default /root/reference/TeaLeaf, or TEALEAF_REF).
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import re
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from exploringsycl_gb300 import deck as dk  # noqa: E402
+from oracle import oracle  # noqa: E402
+from tests.drivers import run_driver  # noqa: E402
+
+DECKS = {
+    "five_state_10x10": dk.five_state(10, end_step=10),
+    "five_state_64x1": dk.five_state(64, end_step=1),
+    "five_state_250x10": dk.five_state(250, end_step=10),
+    "five_state_500x10": dk.five_state(500, end_step=10),
+    "two_state_256x10": dk.two_state(256, end_step=10, max_iters=5000),
+    "five_state_37x53x3": dk.Deck(37, 53, dk.five_state(1).states, end_step=3),
+    "random_seed7_96x2": dk.random_deck(96, seed=7, end_step=2),
+    "inverse_density_40x2": dk.Deck(40, 40, dk.five_state(1).states, end_step=2,
+                                    coefficient="inverse_density"),
+    "jacobi_40x2": dk.five_state(40, end_step=2, max_iters=400, solver="jacobi"),
+    "cheby_64x2": dk.five_state(64, end_step=2, solver="chebyshev", presteps=8),
+    "ppcg_64x2": dk.five_state(64, end_step=2, solver="ppcg", presteps=8),
+}
+
+FORTRAN_OUT = {1: "tea_bm_1.out", 2: "tea_bm_2.out", 3: "tea_bm_3.out"}
+
+
+def fortran_summaries() -> dict:
+    out = {}
+    for bm, name in FORTRAN_OUT.items():
+        text = (oracle.REFERENCE_SOURCES / "Benchmarks" / name).read_text().splitlines()
+        line = text[172]  # line 173: "step: 10 volume mass density energy u"
+        vals = [float(v.replace("D", "E")) for v in line.split()[2:]]
+        out[f"tea_bm_{bm}"] = {"source": f"TeaLeaf/Benchmarks/{name}:173",
+                               "volume": vals[0], "mass": vals[1], "density": vals[2],
+                               "energy": vals[3], "u": vals[4]}
+    return out
+
+
+def main() -> None:
+    oracle.build(with_reference=True)
+    runs = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, d in DECKS.items():
+            r = run_driver(oracle.REF_DRIVER, d, Path(tmp) / name)
+            assert r.returncode == 0, r.stdout[-1000:]
+            runs[name] = {"deck": d.text(), "iterations": r.iterations, "errors": r.errors,
+                          "summaries": [list(s) for s in r.summaries],
+                          "passed": r.passed,
+                          "expected": re.findall(r"^Expected (\S+)", r.stdout, re.M),
+                          "actual": re.findall(r"^Actual\s+(\S+)", r.stdout, re.M)}
+    out = {"generator": "tests/golden/make_golden.py",
+           "driver": "reference TeaLeaf host driver (TeaLeaf/*.c, drivers/*.c, -DNO_MPI) "
+                     "linked with oracle/tl_oracle.c",
+           "runs": runs, "fortran_step10": fortran_summaries()}
+    path = Path(__file__).with_name("reference_driver_runs.json")
+    path.write_text(json.dumps(out, indent=1))
+    print(f"wrote {path}")
+
+
+if __name__ == "__main__":
+    main()
