@@ -1,13 +1,17 @@
 #!/usr/bin/env python3
 """Benchmark of the TeaLeaf CG timestep on GB300.
 
-Workload (default): the two-state deck at 4096 x 4096 cells (background
-density 100 / energy 1e-4, hot rectangle x in [0,1], y in [1,2] at density
-0.1 / energy 25), dt 0.004, conductivity = 1/density, plain FP64 CG with the
-reference's stop rule sqrt(|rr|) < eps = 1e-15 and max_iters 10000. A step is
-one timestep of that deck (TeaLeaf/diffuse.c:23-78): halo update, the CG
-solve, residual / norm / finalise. Timesteps follow one another as in the
-reference run (warm-up steps are timesteps 1..W).
+Default workload (the headline): the seeded random-state deck at 4096 x 4096
+cells (20-60 rectangles and discs, density log-uniform in [0.05, 200], energy
+uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
+1/density; each timestep solved until the FP64 true residual satisfies
+||u0 - A u||_2 <= 1e-10 ||u0||_2, with the mixed-precision Jacobi-PCG solver
+(FP32 inner solve, FP64 refinement). The same timesteps are also solved with
+plain FP64 CG under the same stop rule (the `compare` object). A step is one
+timestep (TeaLeaf/diffuse.c:23-78): halo update, the solve, residual / norm /
+finalise. Timesteps follow one another (warm-up steps are timesteps 1..W).
+`--solver plain --deck two-state` is the drop-in configuration: the
+reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000.
 
 Reported:
   value      device time per timestep (CUDA events on the library's stream,
@@ -15,15 +19,15 @@ Reported:
   e2e        the same timestep through the C ABI with host buffers: density
              and energy copied in from pinned host memory, energy and the
              field summary copied back, inside the timed region
-  roofline   the persistent CG kernel: algorithmic bytes (104 B per interior
-             cell per CG step) / kernel time, against the measured HBM copy
-             bandwidth; plus its FP64 operation rate against the measured
-             FP64 peak (the kernel is bound by FP64 issue on GB300)
+  roofline   the dominant kernel (the persistent inner FP32 CG kernel, or the
+             FP64 CG kernel for plain/cg64): algorithmic bytes / kernel time
+             against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (restatement of the reference's kernels) on
-             this host's cores: CG steps of timestep 1 timed and scaled by
-             the timestep's CG step count
---impl reference times only that CPU path (the reference's algorithm) as a
-bounded sample per step.
+             this host's cores: plain FP64 CG steps of timestep 1 timed and
+             scaled by the CG step count of each timestep under the same stop
+             rule (bit-identical on CPU and GPU)
+--impl reference times only that CPU path (the reference's algorithm: plain
+FP64 CG) as a bounded sample per step.
 
 Multi-GPU: replicas only (one independent chunk per GPU); value is the
 whole-job time per timestep (max over ranks / timesteps of all ranks).
@@ -48,12 +52,21 @@ METRIC = ("s/timestep to 1e-10 FP64 residual @4096²: learned+mixed PCG vs plain
           "HBM GB/s")
 UNIT = "s/timestep"
 BYTES_PER_CELL_STEP = 104          # calc_w 32 + calc_ur 48 + calc_p 24 (FP64)
-FP64_OPS_PER_CELL_STEP = 23        # operations of the exact double-precision CG step
-# dram__bytes_read.sum + dram__bytes_write.sum of the persistent CG kernel
-# per interior cell per CG step, from profiles/cg_persistent_fp64_1024.txt
-# (None until a capture exists).
-NCU_BYTES_PER_CELL_STEP = None
-ITER_FIXTURE = ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json"
+# FP32 inner CG step: phase 1 reads r, p_old, kx, ky and writes p_new, w (24 B);
+# phase 2 reads p_new, w, e, r and writes e, r (24 B); Jacobi adds inv_diag
+# reads in both phases (8 B).
+INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
+FP64_OPS_PER_CELL_STEP = 19        # FP64 instructions per cell of the exact CG step
+# dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
+# each persistent kernel, from one ncu capture (profiles/*.txt).
+NCU_BYTES_PER_CELL_STEP = {
+    "cg_persistent_kernel": 112.3,  # profiles/cg_persistent_fp64_4096.txt (104 + diag 8)
+    "inner_cg_kernel": None,
+}
+ITER_FIXTURES = {"two-state": ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json",
+                 "random": ROOT / "tests" / "golden" / "cg_iterations_random_4096.json"}
+RANDOM_SEED = 1
+REL_TOL = 1e-10
 
 
 def load_peaks() -> dict:
@@ -64,7 +77,7 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-FP64_PEAK_GOPS = 505.0  # measured on GB300: DADD/DMUL/DFMA issue, 152 SMs
+FP64_PEAK_GOPS = 629.0  # GB300: 2 FP64 ops/clk/SM (ncu peak_sustained) x 152 SMs x 2.07 GHz
 
 
 class ClockSampler:
@@ -119,16 +132,33 @@ class ClockSampler:
 MAX_ITERS = 10000
 
 
-def deck_for(size: int):
+def deck_for(size: int, kind: str = "random"):
     from exploringsycl_gb300 import deck as dk
-    return dk.two_state(size, end_step=100, eps=1.0e-15, max_iters=MAX_ITERS)
+    if kind == "two-state":
+        return dk.two_state(size, end_step=100, eps=1.0e-15, max_iters=MAX_ITERS)
+    return dk.random_deck(size, seed=RANDOM_SEED, end_step=100, eps=1.0e-15,
+                          max_iters=MAX_ITERS)
+
+
+def stop_rule(solver: str) -> str:
+    if solver == "plain":
+        return "sqrt(|rr|) < 1e-15 (the reference's absolute rule), max_iters 10000"
+    return f"FP64 true residual ||u0 - A u|| <= {REL_TOL:g} ||u0||"
 
 
 def config_for(args, steps_per_timestep=None) -> dict:
-    return {"workload": f"two-state deck {args.size}x{args.size} cells, plain FP64 CG "
-                        f"(eps 1e-15 absolute, max_iters 10000), consecutive timesteps",
+    deck = ("two-state deck (background rho 100 / e 1e-4, hot rectangle rho 0.1 / e 25)"
+            if args.deck == "two-state" else
+            f"random-state deck (splitmix64 seed {RANDOM_SEED}: 20-60 rectangles and discs, "
+            "rho log-uniform [0.05, 200], e uniform [1e-4, 25])")
+    solver = {"plain": "plain FP64 CG, persistent kernel (run-ahead drop-in)",
+              "cg64": "plain FP64 CG, persistent kernel",
+              "mixed": "FP32 inner CG in FP64 iterative refinement",
+              "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement"}[args.solver]
+    return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "
+                        f"{stop_rule(args.solver)}, consecutive timesteps",
             "cells": args.size * args.size, "halo_depth": 2, "dt": 0.004,
-            "solver": "plain FP64 CG, persistent kernel (run-ahead)",
+            "deck": args.deck, "solver": args.solver, "stop": stop_rule(args.solver),
             "max_iters": MAX_ITERS,
             "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2)",
             "cg_steps_per_timestep": steps_per_timestep}
@@ -136,14 +166,14 @@ def config_for(args, steps_per_timestep=None) -> dict:
 
 # ----------------------------------------------------------------- CPU side
 
-def cpu_sample(size: int, iters: int, threads: int | None = None) -> dict:
+def cpu_sample(size: int, iters: int, kind: str = "random", threads: int | None = None) -> dict:
     """Times `iters` CG steps of timestep 1 with the CPU oracle."""
     from oracle import oracle
     oracle.build(with_reference=False)
     L = oracle.lib()
     if threads:
         L.orc_set_num_threads(threads)
-    ch = oracle.OracleChunk(deck_for(size))
+    ch = oracle.OracleChunk(deck_for(size, kind))
     # timestep 1 set-up, as in cg_timestep
     x, y, hd = ch.x, ch.y, ch.hd
     rx, ry = ch.rx_ry()
@@ -172,9 +202,12 @@ def cpu_sample(size: int, iters: int, threads: int | None = None) -> dict:
     return {"s_per_iter": dt / iters, "cores": L.orc_num_threads(), "iters": iters}
 
 
-def fixture_iterations(size: int) -> list[int] | None:
-    if ITER_FIXTURE.exists():
-        d = json.loads(ITER_FIXTURE.read_text())
+def fixture_iterations(size: int, kind: str) -> list[int] | None:
+    """Plain FP64 CG step counts of consecutive timesteps, recorded from a
+    GPU run (the GPU's FP64 CG is bit-identical to the oracle's)."""
+    p = ITER_FIXTURES[kind]
+    if p.exists():
+        d = json.loads(p.read_text())
         if d.get("size") == size:
             return d["cg_steps"]
     return None
@@ -184,7 +217,7 @@ def run_reference(args, rank: int, world: int) -> None:
     """CPU implementation of the reference's algorithm (the oracle port)."""
     if rank != 0:
         return
-    iters_per_ts = fixture_iterations(args.size)
+    iters_per_ts = fixture_iterations(args.size, args.deck)
     if iters_per_ts is None:
         print(json.dumps({"impl": "reference", "unavailable":
                           f"no CG step counts for {args.size}^2 timesteps recorded yet"}))
@@ -195,7 +228,7 @@ def run_reference(args, rank: int, world: int) -> None:
     per_step = []
     cores = None
     for k in range(args.warmup + args.steps):
-        s = cpu_sample(args.size, args.ref_iters)
+        s = cpu_sample(args.size, args.ref_iters, args.deck)
         cores = s["cores"]
         if k >= args.warmup:
             per_step.append(s["s_per_iter"])
@@ -206,7 +239,7 @@ def run_reference(args, rank: int, world: int) -> None:
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_for(args, ts_steps),
+        "config": dict(config_for(args, ts_steps), solver="plain FP64 CG (CPU oracle)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{args.ref_iters} CG steps of timestep 1 per step, "
                                    f"scaled by {mean_steps:.1f} CG steps per timestep"},
@@ -227,50 +260,69 @@ def max_over_ranks(values: list[float], dist) -> list[float]:
     return [float(v) for v in t]
 
 
+class Stepper:
+    """One chunk and the timestep of the chosen solver."""
+
+    def __init__(self, args, solver: str, ctx):
+        from exploringsycl_gb300.chunk import GpuChunk
+        self.solver = solver
+        self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
+        self.ctx = ctx
+        self.inner_tol = args.inner_tol
+
+    def step(self) -> dict:
+        """Runs one timestep; returns the dominant kernel's time and steps."""
+        if self.solver == "plain":
+            steps = self.chunk.cg_timestep()
+            st = self.ctx.solve_stats()
+            return {"kernel_ms": st.kernel_ms, "kernel_steps": steps, "cg_steps": steps}
+        rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL, inner_tol=self.inner_tol)
+        return {"kernel_ms": rep["inner_kernel_ms"],
+                "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
+                "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
+
+
+def timed_steps(stepper, steps: int, stream, barrier, sample_clocks: bool, device: int):
+    import torch
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(device) if sample_clocks else None
+    if sampler:
+        sampler.start()
+    launches0 = stepper.ctx.launches()
+    per = []
+    ev0.record(stream)
+    for _ in range(steps):
+        per.append(stepper.step())
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    barrier()
+    return ev0.elapsed_time(ev1), per, stepper.ctx.launches() - launches0, clocks
+
+
 def run_ours(args, rank: int, world: int, dist) -> None:
-    import numpy as np
     import torch
 
     from exploringsycl_gb300 import Context
-    from exploringsycl_gb300.chunk import GpuChunk
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     ctx = Context(device=local)
-    chunk = GpuChunk(deck_for(args.size), ctx=ctx)
+    main = Stepper(args, args.solver, ctx)
+    chunk = main.chunk
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    all_steps = []
-    for _ in range(args.warmup):
-        all_steps.append(chunk.cg_timestep())
+    warm = [main.step() for _ in range(args.warmup)]
     torch.cuda.synchronize()
-
-    barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    sampler = ClockSampler(local)
-    sampler.start()
-    launches0 = ctx.launches()
-    kernel_ms, cg_steps = [], []
-    ev0.record(stream)
-    for _ in range(args.steps):
-        chunk.cg_timestep()
-        st = ctx.solve_stats()
-        kernel_ms.append(st.kernel_ms)
-        cg_steps.append(st.steps)
-        all_steps.append(st.steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    launches = ctx.launches() - launches0
-    total_ms = ev0.elapsed_time(ev1)
-    barrier()
+    total_ms, per, launches, clocks = timed_steps(main, args.steps, stream, barrier, True, local)
 
     # e2e: host buffers in, results out, through the C ABI.
     n = chunk.n
@@ -281,12 +333,13 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     lib.tl_copy_to_host(ctx.h, h_density.data_ptr(), chunk.f["density"], n)
     lib.tl_copy_to_host(ctx.h, h_energy.data_ptr(), chunk.f["energy"], n)
     e2e_times = []
+    summary = None
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         lib.tl_copy_to_device(ctx.h, chunk.f["density"], h_density.data_ptr(), n)
         lib.tl_copy_to_device(ctx.h, chunk.f["energy"], h_energy.data_ptr(), n)
-        chunk.cg_timestep()
+        main.step()
         summary = chunk.summary()
         lib.tl_copy_to_host(ctx.h, h_out.data_ptr(), chunk.f["energy"], n)
         torch.cuda.synchronize()
@@ -294,51 +347,90 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         h_energy.copy_(h_out)
     barrier()
 
-    total_ms, e2e_mean = max_over_ranks([total_ms, statistics.mean(e2e_times)], dist)
+    # The same timesteps with plain FP64 CG under the same stop rule.
+    compare = None
+    if args.compare and args.solver != "plain":
+        ctx2 = Context(device=local)
+        plain = Stepper(args, "cg64", ctx2)
+        cwarm = [plain.step() for _ in range(args.warmup)]
+        stream2 = torch.cuda.ExternalStream(ctx2.stream(), device=local)
+        c_ms, c_per, _, _ = timed_steps(plain, args.steps, stream2, barrier, False, local)
+        compare = {"solver": "plain FP64 CG, same stop rule",
+                   "value": c_ms / 1e3 / args.steps, "unit": UNIT,
+                   "cg_steps_per_timestep": [p["cg_steps"] for p in cwarm + c_per],
+                   "speedup": (c_ms / args.steps) / (total_ms / args.steps)}
+        if args.dump_iterations:
+            Path(args.dump_iterations).write_text(json.dumps(
+                {"size": args.size, "deck": args.deck, "stop": stop_rule("cg64"),
+                 "cg_steps": compare["cg_steps_per_timestep"]}))
+        plain.chunk.close()
 
+    total_ms, e2e_mean = max_over_ranks([total_ms, statistics.mean(e2e_times)], dist)
     if rank != 0:
         ctx.close()
         return
     value = total_ms / 1e3 / (args.steps * world)
     cells = args.size * args.size
-    k_ms = statistics.mean(kernel_ms)
-    k_steps = statistics.mean(cg_steps)
+    k_ms = statistics.mean(p["kernel_ms"] for p in per)
+    k_steps = statistics.mean(p["kernel_steps"] for p in per)
     peaks = load_peaks()
-    achieved = BYTES_PER_CELL_STEP * cells * k_steps / (k_ms * 1e-3) / 1e9
-    traffic = (NCU_BYTES_PER_CELL_STEP * cells * k_steps
-               if NCU_BYTES_PER_CELL_STEP is not None else None)
-    fp64_gops = FP64_OPS_PER_CELL_STEP * cells * k_steps / (k_ms * 1e-3) / 1e9
-    cpu = cpu_sample(args.size, args.cpu_iters) if not args.skip_cpu else None
+    if args.solver in ("plain", "cg64"):
+        kernel, bpc = "cg_persistent_kernel", BYTES_PER_CELL_STEP
+    else:
+        kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
+    achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9
+    traffic = None
+    if NCU_BYTES_PER_CELL_STEP.get(kernel) is not None:
+        traffic = NCU_BYTES_PER_CELL_STEP[kernel] * cells * k_steps
+    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+            "peak_source": peaks["source"], "traffic": traffic, "bytes_per_cell_step": bpc,
+            "kernel_ms_per_step_avg": k_ms, "kernel_steps_per_timestep": k_steps}
+    if kernel == "cg_persistent_kernel":
+        gops = FP64_OPS_PER_CELL_STEP * cells * k_steps / (k_ms * 1e-3) / 1e9
+        roof.update({"fp64_gops": gops, "fp64_peak_gops": FP64_PEAK_GOPS,
+                     "fp64_frac": gops / FP64_PEAK_GOPS})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_for(args, cg_steps),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.solver in ("plain", "cg64") else "f32 inner / f64 outer",
+        "data": "synthetic",
+        "config": config_for(args, [p["cg_steps"] for p in warm + per]),
         "e2e": {"value": e2e_mean / world, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8 + 32,
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "cg_persistent_kernel",
-                     "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                     "traffic": traffic, "bytes_per_cell_step": BYTES_PER_CELL_STEP,
-                     "kernel_ms_per_launch": k_ms, "cg_steps_per_launch": k_steps,
-                     "fp64_gops": fp64_gops, "fp64_peak_gops": FP64_PEAK_GOPS,
-                     "fp64_frac": fp64_gops / FP64_PEAK_GOPS},
+        "roofline": roof,
         "clocks": clocks,
     }
-    if cpu is not None:
+    reports = [p["report"] for p in per if "report" in p]
+    if reports:
+        line["solve"] = {
+            "outer_steps": [r["outer_steps"] for r in reports],
+            "inner_steps": [r["inner_steps"] for r in reports],
+            "fallback_events": sum(r["fallback_events"] for r in reports),
+            "final_rel_residual_max": max(r["final_rel_residual"] for r in reports),
+            "error_vs_fp64": "every timestep stops at an FP64 true residual <= 1e-10 relative "
+                             "(tests/test_gpu_mixed.py: u within 1e-7 of the FP64 oracle CG)"}
+    if compare:
+        line["compare"] = compare
+    if not args.skip_cpu:
+        cpu = cpu_sample(args.size, args.cpu_iters, args.deck)
+        ref_steps = (compare["cg_steps_per_timestep"][args.warmup:] if compare
+                     else [p["cg_steps"] for p in per])
+        mean_steps = statistics.mean(ref_steps)
         line["cpu_baseline"] = {
-            "value": cpu["s_per_iter"] * statistics.mean(cg_steps), "unit": UNIT,
-            "cores": cpu["cores"], "kind": "port",
-            "sample": f"{cpu['iters']} CG steps of timestep 1 on the CPU oracle, scaled by "
-                      f"{statistics.mean(cg_steps):.1f} CG steps per timestep"}
-    if args.dump_iterations:
+            "value": cpu["s_per_iter"] * mean_steps, "unit": UNIT, "cores": cpu["cores"],
+            "kind": "port",
+            "sample": f"{cpu['iters']} plain FP64 CG steps of timestep 1 on the CPU oracle, "
+                      f"scaled by {mean_steps:.1f} CG steps per timestep (same stop rule)"}
+    if args.dump_iterations and args.solver == "plain":
         Path(args.dump_iterations).write_text(json.dumps(
-            {"size": args.size, "cg_steps": [int(s) for s in all_steps],
-             "summary_after": summary}))
+            {"size": args.size, "deck": args.deck, "stop": stop_rule("plain"),
+             "cg_steps": [p["cg_steps"] for p in warm + per], "summary_after": summary}))
     print(json.dumps(line))
-    ctx.close()
+    chunk.close()
 
 
 def main() -> None:
@@ -348,6 +440,12 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--deck", choices=["random", "two-state"], default="random")
+    ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "cg64", "plain"],
+                    default="mixed-jacobi")
+    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="skip the plain FP64 CG run of the same timesteps")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-iters", type=int, default=5)
     ap.add_argument("--ref-iters", type=int, default=5)

@@ -36,6 +36,26 @@ class TLSolveStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_float), ("steps", C.c_int), ("kernel_launches", C.c_int)]
 
 
+class TLSolveParams(C.Structure):
+    _fields_ = [("method", C.c_int), ("rel_tol", C.c_double), ("inner_tol", C.c_double),
+                ("max_inner", C.c_int), ("max_outer", C.c_int), ("stall_factor", C.c_double),
+                ("max_fallback", C.c_int)]
+
+
+class TLSolveReport(C.Structure):
+    _fields_ = [("outer_steps", C.c_int), ("inner_steps", C.c_int),
+                ("fallback_events", C.c_int), ("fallback_steps", C.c_int),
+                ("initial_rel_residual", C.c_double), ("final_rel_residual", C.c_double),
+                ("device_ms", C.c_float), ("inner_kernel_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI = 0, 1, 2
+METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI}
+
+
 class TLState(C.Structure):
     _fields_ = [("density", C.c_double), ("energy", C.c_double), ("x_min", C.c_double),
                 ("y_min", C.c_double), ("x_max", C.c_double), ("y_max", C.c_double),
@@ -75,6 +95,8 @@ SIGNATURES: dict[str, list] = {
     "tl_cheby_iterate": [_I, _I, _I, _D, _D, _P, _P, _P, _P, _P, _P, _P],
     "tl_ppcg_init": [_I, _I, _I, _D, _P, _P],
     "tl_ppcg_inner_iteration": [_I, _I, _I, _D, _D, _D, _P, _P, _P, _P, _P],
+    "tl_solve": [_I, _I, _I, _I, _D, _D, C.POINTER(TLSolveParams), _P, _P, _P, _P, _P, _P, _P,
+                 _P, _P, C.POINTER(TLSolveReport)],
 }
 
 # Entry points that do not take a context first.

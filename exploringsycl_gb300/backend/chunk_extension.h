@@ -23,4 +23,7 @@ typedef struct ChunkExtension {
   double* ra_pw;          /* host: pw of each device step */
   double* ra_rrn;         /* host: rrn of each device step */
   int ra_cap;
+  int replace_method;     /* -1, or a TL_METHOD_* that replaces the CG solve */
+  double replace_rel_tol; /* its relative FP64 true-residual target */
+  double replace_inner_tol;
 } ChunkExtension;

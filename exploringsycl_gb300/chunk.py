@@ -13,7 +13,8 @@ import math
 
 import numpy as np
 
-from . import CONDUCTIVITY, Context, TLState, check
+from . import (CONDUCTIVITY, METHODS, Context, TLSolveParams, TLSolveReport, TLState,
+               check)
 from .deck import Deck
 
 GEOMETRY = {"rectangle": 0, "circular": 1, "point": 2}
@@ -110,6 +111,25 @@ class GpuChunk:
         self.last_steps = steps.value
         self.solve_finished()
         return steps.value
+
+    def solve_timestep(self, method: str = "mixed", rel_tol: float = 1e-10,
+                       inner_tol: float = 1e-5, max_inner: int = 20000, max_outer: int = 12,
+                       stall_factor: float = 0.5, max_fallback: int = 20000) -> dict:
+        """One timestep solved to a relative FP64 true residual with one of
+        the solver-replacement methods (cg64 | mixed | mixed-jacobi)."""
+        x, y, hd, f = self.x, self.y, self.hd, self.f
+        rx, ry = self.rx_ry()
+        self.halos(["energy", "density"], 2)
+        prm = TLSolveParams(METHODS[method], rel_tol, inner_tol, max_inner, max_outer,
+                            stall_factor, max_fallback)
+        rep = TLSolveReport()
+        self.call("tl_solve", x, y, hd, self.coefficient, rx, ry, C.byref(prm), f["p"], f["r"],
+                  f["u"], f["u0"], f["w"], f["kx"], f["ky"], f["density"], f["energy"],
+                  C.byref(rep))
+        self.last_report = rep.as_dict()
+        self.last_steps = rep.inner_steps + rep.fallback_steps
+        self.solve_finished()
+        return self.last_report
 
     def solve_finished(self) -> None:
         """TeaLeaf/drivers/solve_finished_driver.c:7-43."""

@@ -87,6 +87,8 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_status);
   cudaFree(ctx->d_hist);
   cudaFree(ctx->d_stage);
+  cudaFree(ctx->d_diag);
+  cudaFree(ctx->d_f32);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
   if (ctx->h_steps) cudaFreeHost(ctx->h_steps);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -152,6 +154,17 @@ int tl_ensure_stage(tl_context* ctx, size_t n) {
   ctx->stage_cap = 0;
   TL_CUDA(cudaMalloc(&ctx->d_stage, n * sizeof(double)));
   ctx->stage_cap = n;
+  return TL_OK;
+}
+
+int tl_ensure_diag(tl_context* ctx, size_t n) {
+  if (n <= ctx->diag_cap) return TL_OK;
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->d_diag);
+  ctx->d_diag = nullptr;
+  ctx->diag_cap = 0;
+  TL_CUDA(cudaMalloc(&ctx->d_diag, n * sizeof(double)));
+  ctx->diag_cap = n;
   return TL_OK;
 }
 

@@ -13,7 +13,7 @@
  *    memory, so one launch and one stream synchronisation return a dot
  *    product (the reference issues 1 + ceil(log64 n) kernels and a blocking
  *    host read, TeaLeaf/c_kernels/sycl/sycl_shared.hpp:35-79);
- *  - the persistent CG kernel: one 512-thread block per SM (cooperative
+ *  - the persistent CG kernel: one 1024-thread block per SM (cooperative
  *    launch), three grid barriers per CG step, scalars alpha/beta computed
  *    redundantly (and identically) by every block.
  */
@@ -30,7 +30,7 @@ namespace {
 
 constexpr int kMapThreads = 256;
 constexpr int kRedThreads = 256;
-constexpr int kPersistThreads = 512;
+constexpr int kPersistThreads = 1024;
 
 /* ------------------------------------------------------------ helpers */
 
@@ -613,7 +613,7 @@ struct CgPersistParams {
   int x, y, hd, ntiles, max_iters;
   double eps, rro;
   double *u, *p, *r, *w;
-  const double *kx, *ky;
+  const double *kx, *ky, *diag;
   double *part_w, *part_r;
   double *pw_hist, *rrn_hist;
   unsigned* sync;
@@ -621,55 +621,226 @@ struct CgPersistParams {
   int* steps_out;
 };
 
+/* Diagonal of the operator, (1 + (kx[i+1]+kx[i])) + (ky[i+x]+ky[i]), computed
+ * once per solve with exactly the grouping of TeaLeaf/shared.h:60-61 so that
+ * diag*a equals the first term of the operator bit for bit. */
+struct DiagOp {
+  int x, y, hd;
+  const double *kx, *ky;
+  double* diag;
+  __device__ void operator()(unsigned i, int kk, int jj) const {
+    if (interior(kk, jj, x, y, hd))
+      diag[i] = 1.0 + (kx[i + 1] + kx[i]) + (ky[i + x] + ky[i]);
+  }
+};
+
+/* Sums of 8 consecutive 64-cell groups held by one warp, two cells per lane
+ * per group (v[g] = cell 2*lane + cell 2*lane+1 of group g), in the
+ * reference's tree order. Instead of a full butterfly per group (every lane
+ * adding at every level), the warp halves its set of groups at each of the
+ * first three levels (lane pairs exchange the halves they do not keep), then
+ * finishes with two butterfly levels: the same pairs are added at every
+ * level, but each level costs 4, 2, 1, 1, 1 additions per lane instead of 8.
+ * Returns the total of group ((lane&1)<<2 | (lane&2) | (lane>>2&1)); lanes
+ * with equal low three bits hold the same group. */
+__device__ __forceinline__ double warp_sum8_groups(const double v[8], int lane) {
+  const bool h1 = lane & 1, h2 = lane & 2, h4 = lane & 4;
+  double a[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double send = h1 ? v[k] : v[4 + k];
+    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 1);
+    a[k] = (h1 ? v[4 + k] : v[k]) + recv;
+  }
+  double b[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double send = h2 ? a[k] : a[2 + k];
+    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 2);
+    b[k] = (h2 ? a[2 + k] : a[k]) + recv;
+  }
+  const double send = h4 ? b[0] : b[1];
+  const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 4);
+  double c = (h4 ? b[1] : b[0]) + recv;
+  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 8);
+  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 16);
+  return c;
+}
+
+__device__ __forceinline__ int warp_sum8_group_of_lane(int lane) {
+  return ((lane & 1) << 2) | (lane & 2) | ((lane >> 2) & 1);
+}
+
+constexpr int kWarpsPerTile = TL_GROUP / 8;  /* 8 warps x 8 groups = one tile */
+
+/* w = A p for the two cells i0, i0+1 of a lane (i0 even), contributions
+ * c = w*p (0 outside the interior). kVec: the row length x is even, so the
+ * pair lies in one row and every pair load is 16-byte aligned; the left and
+ * right neighbours come from the adjacent lanes. Otherwise scalar loads. */
+template <bool kVec>
+__device__ __forceinline__ void w_pair(const CgPersistParams& P, unsigned i0, unsigned len,
+                                       int lane, double c[2]) {
+  const int x = P.x, y = P.y, hd = P.hd;
+  c[0] = 0.0;
+  c[1] = 0.0;
+  if constexpr (kVec) {
+    const int jj = (int)(i0 / (unsigned)x);
+    const int kk0 = (int)(i0 - (unsigned)jj * (unsigned)x);
+    const bool row = i0 < len && jj >= hd && jj < y - hd;
+    double2 pc = make_double2(0.0, 0.0), pu = pc, pd = pc, kxp = pc, kyp = pc, kyu = pc,
+            dg = pc;
+    if (row) {
+      pc = __ldcg(reinterpret_cast<const double2*>(P.p + i0));
+      pu = __ldcg(reinterpret_cast<const double2*>(P.p + i0 + x));
+      pd = __ldcg(reinterpret_cast<const double2*>(P.p + i0 - x));
+      kxp = __ldg(reinterpret_cast<const double2*>(P.kx + i0));
+      kyp = __ldg(reinterpret_cast<const double2*>(P.ky + i0));
+      kyu = __ldg(reinterpret_cast<const double2*>(P.ky + i0 + x));
+      dg = __ldg(reinterpret_cast<const double2*>(P.diag + i0));
+    }
+    double pl = __shfl_up_sync(TL_FULL_MASK, pc.y, 1);
+    double pr = __shfl_down_sync(TL_FULL_MASK, pc.x, 1);
+    double kx2 = __shfl_down_sync(TL_FULL_MASK, kxp.x, 1);
+    const bool in0 = row && kk0 >= hd && kk0 < x - hd;
+    const bool in1 = row && kk0 + 1 >= hd && kk0 + 1 < x - hd;
+    if (lane == 0 && in0) pl = __ldcg(P.p + i0 - 1);
+    if (lane == 31 && in1) {
+      pr = __ldcg(P.p + i0 + 2);
+      kx2 = __ldg(P.kx + i0 + 2);
+    }
+    if (in0) {
+      const double s0 = dg.x * pc.x - (kxp.y * pc.y + kxp.x * pl) - (kyu.x * pu.x + kyp.x * pd.x);
+      P.w[i0] = s0;
+      c[0] = s0 * pc.x;
+    }
+    if (in1) {
+      const double s1 = dg.y * pc.y - (kx2 * pr + kxp.y * pc.x) - (kyu.y * pu.y + kyp.y * pd.y);
+      P.w[i0 + 1] = s1;
+      c[1] = s1 * pc.y;
+    }
+  } else {
+    const double* __restrict__ kx = P.kx;
+    const double* __restrict__ ky = P.ky;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const unsigned i = i0 + h;
+      if (i < len) {
+        const int jj = (int)(i / (unsigned)x);
+        const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+        if (interior(kk, jj, x, y, hd)) {
+          const double pc = __ldcg(P.p + i);
+          const double s = P.diag[i] * pc -
+                           (kx[i + 1] * __ldcg(P.p + i + 1) + kx[i] * __ldcg(P.p + i - 1)) -
+                           (ky[i + x] * __ldcg(P.p + i + x) + ky[i] * __ldcg(P.p + i - x));
+          P.w[i] = s;
+          c[h] = s * pc;
+        }
+      }
+    }
+  }
+}
+
+/* u += alpha p, r -= alpha w for the two cells of a lane; c = r*r. */
+template <bool kVec>
+__device__ __forceinline__ void ur_pair(const CgPersistParams& P, unsigned i0, unsigned len,
+                                        double alpha, double c[2]) {
+  const int x = P.x, y = P.y, hd = P.hd;
+  c[0] = 0.0;
+  c[1] = 0.0;
+  if constexpr (kVec) {
+    const int jj = (int)(i0 / (unsigned)x);
+    const int kk0 = (int)(i0 - (unsigned)jj * (unsigned)x);
+    if (!(i0 < len && jj >= hd && jj < y - hd)) return;
+    const bool in0 = kk0 >= hd && kk0 < x - hd;
+    const bool in1 = kk0 + 1 >= hd && kk0 + 1 < x - hd;
+    if (!in0 && !in1) return;
+    const double2 uu = __ldcg(reinterpret_cast<const double2*>(P.u + i0));
+    const double2 pp = __ldcg(reinterpret_cast<const double2*>(P.p + i0));
+    const double2 rr = __ldcg(reinterpret_cast<const double2*>(P.r + i0));
+    const double2 ww = __ldcg(reinterpret_cast<const double2*>(P.w + i0));
+    if (in0 && in1) {
+      const double2 un = make_double2(uu.x + alpha * pp.x, uu.y + alpha * pp.y);
+      const double2 rn = make_double2(rr.x - alpha * ww.x, rr.y - alpha * ww.y);
+      *reinterpret_cast<double2*>(P.u + i0) = un;
+      *reinterpret_cast<double2*>(P.r + i0) = rn;
+      c[0] = rn.x * rn.x;
+      c[1] = rn.y * rn.y;
+    } else if (in0) {
+      P.u[i0] = uu.x + alpha * pp.x;
+      const double rv = rr.x - alpha * ww.x;
+      P.r[i0] = rv;
+      c[0] = rv * rv;
+    } else {
+      P.u[i0 + 1] = uu.y + alpha * pp.y;
+      const double rv = rr.y - alpha * ww.y;
+      P.r[i0 + 1] = rv;
+      c[1] = rv * rv;
+    }
+  } else {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const unsigned i = i0 + h;
+      if (i < len) {
+        const int jj = (int)(i / (unsigned)x);
+        const int kk = (int)(i - (unsigned)jj * (unsigned)x);
+        if (interior(kk, jj, x, y, hd)) {
+          P.u[i] = __ldcg(P.u + i) + alpha * __ldcg(P.p + i);
+          const double rv = __ldcg(P.r + i) - alpha * __ldcg(P.w + i);
+          P.r[i] = rv;
+          c[h] = rv * rv;
+        }
+      }
+    }
+  }
+}
+
 /* One CG step loop of TeaLeaf/drivers/cg_driver.c:18-25 with the kernels of
- * TeaLeaf/c_kernels/sycl/cg.cpp:137-281, all on the device. Each block owns
- * tiles blockIdx.x, blockIdx.x + gridDim.x, ... in every phase. The p halo
- * cells that the stencil reads (depth 1 on each face) are written by the
- * owner of the adjacent interior cell in the p update, which yields the
- * same values as the reference's halo update; corner and outer halo cells
- * are brought up to date by the exact halo update launched after the loop. */
+ * TeaLeaf/c_kernels/sycl/cg.cpp:137-281, all on the device. A block of 1024
+ * threads works on 4 tiles at a time (8 warps per tile, 8 groups of 64
+ * cells per warp); blocks own tiles blockIdx.x*4 + k*gridDim.x*4 in every
+ * phase. The p halo cells that the stencil reads (depth 1 on each face) are
+ * written by the owner of the adjacent interior cell in the p update, which
+ * yields the same values as the reference's halo update; corner and outer
+ * halo cells are brought up to date by the exact halo update launched after
+ * the loop. */
+template <bool kVec>
 __global__ void __launch_bounds__(kPersistThreads, 1)
 cg_persistent_kernel(CgPersistParams P) {
-  __shared__ double s_group[TL_GROUP];
+  constexpr int kSub = kPersistThreads / 32 / kWarpsPerTile;  /* tiles per pass */
+  __shared__ double s_group[kSub][TL_GROUP];
   __shared__ double s_scratch[TL_RED_SCRATCH];
   const int x = P.x, y = P.y, hd = P.hd;
   const unsigned len = (unsigned)x * (unsigned)y;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
-  const double* __restrict__ kx = P.kx;
-  const double* __restrict__ ky = P.ky;
+  const int sub = warp / kWarpsPerTile;       /* which tile of the pass */
+  const int wt = warp % kWarpsPerTile;        /* warp within the tile */
+  const int my_group = warp_sum8_group_of_lane(lane);
   double rro = P.rro;
   int steps = 0;
+  const int stride = gridDim.x * kSub;
 
   for (int k = 0; k < P.max_iters; ++k) {
     /* ---- w = A p, pw partials (cg_calc_w) */
-    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-      const unsigned base = (unsigned)tile * TL_TILE;
-      for (int g = warp; g < TL_GROUP; g += nwarps) {
-        const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
-        double c0 = 0.0, c1 = 0.0;
+    for (int t0 = blockIdx.x * kSub; t0 < P.ntiles; t0 += stride) {
+      const int tile = t0 + sub;
+      if (tile < P.ntiles) {
+        const unsigned base = (unsigned)tile * TL_TILE + (unsigned)wt * 8 * TL_GROUP;
+        double v[8];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const unsigned i = i0 + h;
-          if (i < len) {
-            const int jj = (int)(i / (unsigned)x);
-            const int kk = (int)(i - (unsigned)jj * (unsigned)x);
-            if (interior(kk, jj, x, y, hd)) {
-              const double s = smvp(L2Load{P.p}, kx, ky, i, x);
-              P.w[i] = s;
-              const double c = s * __ldcg(P.p + i);
-              if (h == 0) c0 = c; else c1 = c;
-            }
-          }
+        for (int g = 0; g < 8; ++g) {
+          const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
+          double c[2];
+          w_pair<kVec>(P, i0, len, lane, c);
+          v[g] = c[0] + c[1];
         }
-        const double v = tl_tree64(c0, c1);
-        if (lane == 0) s_group[g] = v;
+        const double gs = warp_sum8_groups(v, lane);
+        if (lane < 8) s_group[sub][wt * 8 + my_group] = gs;
       }
       __syncthreads();
-      if (warp == 0) {
-        const double v = tl_tree64(s_group[2 * lane], s_group[2 * lane + 1]);
-        if (lane == 0) P.part_w[tile] = v;
+      if (wt == 0 && tile < P.ntiles) {
+        const double t = tl_tree64(s_group[sub][2 * lane], s_group[sub][2 * lane + 1]);
+        if (lane == 0) P.part_w[tile] = t;
       }
       __syncthreads();
     }
@@ -678,33 +849,25 @@ cg_persistent_kernel(CgPersistParams P) {
     const double alpha = rro / pw;
 
     /* ---- u += alpha p, r -= alpha w, rrn partials (cg_calc_ur) */
-    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-      const unsigned base = (unsigned)tile * TL_TILE;
-      for (int g = warp; g < TL_GROUP; g += nwarps) {
-        const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
-        double c0 = 0.0, c1 = 0.0;
+    for (int t0 = blockIdx.x * kSub; t0 < P.ntiles; t0 += stride) {
+      const int tile = t0 + sub;
+      if (tile < P.ntiles) {
+        const unsigned base = (unsigned)tile * TL_TILE + (unsigned)wt * 8 * TL_GROUP;
+        double v[8];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const unsigned i = i0 + h;
-          if (i < len) {
-            const int jj = (int)(i / (unsigned)x);
-            const int kk = (int)(i - (unsigned)jj * (unsigned)x);
-            if (interior(kk, jj, x, y, hd)) {
-              P.u[i] = __ldcg(P.u + i) + alpha * __ldcg(P.p + i);
-              const double rv = __ldcg(P.r + i) - alpha * __ldcg(P.w + i);
-              P.r[i] = rv;
-              const double c = rv * rv;
-              if (h == 0) c0 = c; else c1 = c;
-            }
-          }
+        for (int g = 0; g < 8; ++g) {
+          const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
+          double c[2];
+          ur_pair<kVec>(P, i0, len, alpha, c);
+          v[g] = c[0] + c[1];
         }
-        const double v = tl_tree64(c0, c1);
-        if (lane == 0) s_group[g] = v;
+        const double gs = warp_sum8_groups(v, lane);
+        if (lane < 8) s_group[sub][wt * 8 + my_group] = gs;
       }
       __syncthreads();
-      if (warp == 0) {
-        const double v = tl_tree64(s_group[2 * lane], s_group[2 * lane + 1]);
-        if (lane == 0) P.part_r[tile] = v;
+      if (wt == 0 && tile < P.ntiles) {
+        const double t = tl_tree64(s_group[sub][2 * lane], s_group[sub][2 * lane + 1]);
+        if (lane == 0) P.part_r[tile] = t;
       }
       __syncthreads();
     }
@@ -717,9 +880,9 @@ cg_persistent_kernel(CgPersistParams P) {
     }
 
     /* ---- p = beta p + r (cg_calc_p), plus the depth-1 face halos of p */
-    for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-      const unsigned base = (unsigned)tile * TL_TILE;
-      for (unsigned t = threadIdx.x; t < TL_TILE; t += blockDim.x) {
+    for (int t0 = blockIdx.x * kSub; t0 < P.ntiles; t0 += stride) {
+      const unsigned base = (unsigned)t0 * TL_TILE;
+      for (unsigned t = threadIdx.x; t < (unsigned)kSub * TL_TILE; t += blockDim.x) {
         const unsigned i = base + t;
         if (i >= len) break;
         const int jj = (int)(i / (unsigned)x);
@@ -1019,48 +1182,42 @@ extern "C" int tl_ppcg_inner_iteration(tl_context* ctx, int x, int y, int hd,
   return launch_map(ctx, PpcgCalcSdOp{x, y, hd, alpha, beta, sd, r}, x, y);
 }
 
-extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficient,
-                           double rx, double ry, double eps, int max_iters, double* p,
-                           double* r, double* u, double* u0, double* w, double* kx,
-                           double* ky, const double* density, const double* energy,
-                           double* rro0, double* pw_hist, double* rrn_hist, int* steps) {
-  CTX_OK(ctx);
-  DIMS_OK(x, y, hd);
-  TL_REQUIRE(rro0 && steps && (max_iters == 0 || (pw_hist && rrn_hist)),
-             "null output of tl_cg_solve");
-  TL_REQUIRE(max_iters >= 0, "negative max_iters");
+/* The persistent CG loop from a prepared state (r, p with its face halos,
+ * rro = r.r), as in tl_cg_solve after its initialisation; also used by the
+ * mixed-precision solver to finish in FP64. Leaves u and p with their final
+ * depth-1 halos. pw_hist/rrn_hist (host) may be null. */
+int tl_internal_cg64_loop(tl_context* ctx, int x, int y, int hd, double eps, int max_iters,
+                          double* p, double* r, double* u, double* w, const double* kx,
+                          const double* ky, double rro, double* pw_hist, double* rrn_hist,
+                          int* steps) {
   *steps = 0;
-
-  /* cg_init_driver: init kernels, halo of u and p, u0 = u. */
-  double rro = 0.0;
-  int rc = cg_init_impl(ctx, x, y, hd, coefficient, rx, ry, p, r, u, w, kx, ky, density,
-                        energy, &rro);
-  if (rc != TL_OK) return rc;
-  *rro0 += rro;
   double* up[2] = {u, p};
-  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
-  if (rc != TL_OK) return rc;
-  rc = launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
-  if (rc != TL_OK) return rc;
-  if (max_iters == 0) return TL_OK;
-
+  if (max_iters <= 0) return TL_OK;
   const size_t ntiles = tl_num_tiles(x, y);
-  rc = tl_ensure_partials(ctx, ntiles);
+  int rc = tl_ensure_partials(ctx, ntiles);
   if (rc != TL_OK) return rc;
   rc = tl_ensure_history(ctx, (size_t)max_iters);
   if (rc != TL_OK) return rc;
+  rc = tl_ensure_diag(ctx, (size_t)x * y);
+  if (rc != TL_OK) return rc;
+  rc = launch_map(ctx, DiagOp{x, y, hd, kx, ky, ctx->d_diag}, x, y);
+  if (rc != TL_OK) return rc;
 
   int per_sm = 0;
-  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_persistent_kernel,
-                                                        kPersistThreads, 0));
+  /* Pair loads need an even row length (16-byte aligned pairs in one row). */
+  const void* kernel = (x % 2 == 0) ? (const void*)cg_persistent_kernel<true>
+                                    : (const void*)cg_persistent_kernel<false>;
+  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, 0));
   TL_REQUIRE(per_sm >= 1, "persistent CG kernel cannot be resident");
+  const int tiles_per_block = kPersistThreads / 32 / kWarpsPerTile;
   int grid = ctx->num_sms * std::min(per_sm, 1);
-  if ((size_t)grid > ntiles) grid = (int)ntiles;
+  const int needed = (int)((ntiles + tiles_per_block - 1) / tiles_per_block);
+  if (grid > needed) grid = needed;
 
   CgPersistParams P;
   P.x = x; P.y = y; P.hd = hd; P.ntiles = (int)ntiles; P.max_iters = max_iters;
   P.eps = eps; P.rro = rro;
-  P.u = u; P.p = p; P.r = r; P.w = w; P.kx = kx; P.ky = ky;
+  P.u = u; P.p = p; P.r = r; P.w = w; P.kx = kx; P.ky = ky; P.diag = ctx->d_diag;
   P.part_w = ctx->d_part; P.part_r = ctx->d_part + ctx->part_cap;
   P.pw_hist = ctx->d_hist; P.rrn_hist = ctx->d_hist + ctx->hist_cap;
   P.sync = ctx->d_sync; P.status = ctx->d_status; P.steps_out = ctx->d_steps;
@@ -1070,8 +1227,8 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
   ctx->h_steps[0] = -1;
   void* args[] = {&P};
   TL_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
-  TL_CUDA(cudaLaunchCooperativeKernel((const void*)cg_persistent_kernel, dim3(grid),
-                                      dim3(kPersistThreads), args, 0, ctx->stream));
+  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(kPersistThreads), args, 0,
+                                      ctx->stream));
   TL_CHECK_LAUNCH(ctx);
   TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
   /* Final state of the u and p halos, as after the reference's last halo
@@ -1087,7 +1244,7 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
   }
   const int n = ((volatile int*)ctx->h_steps)[0];
   TL_REQUIRE(n >= 0 && n <= max_iters, "persistent CG kernel did not report its steps");
-  if (n > 0) {
+  if (n > 0 && pw_hist && rrn_hist) {
     TL_CUDA(cudaMemcpyAsync(pw_hist, ctx->d_hist, (size_t)n * sizeof(double),
                             cudaMemcpyDeviceToHost, ctx->stream));
     TL_CUDA(cudaMemcpyAsync(rrn_hist, ctx->d_hist + ctx->hist_cap, (size_t)n * sizeof(double),
@@ -1101,6 +1258,64 @@ extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficien
   ctx->last_solve.steps = n;
   ctx->last_solve.kernel_launches = 1;
   return TL_OK;
+}
+
+/* CG from the current iterate u towards A u = u0: r = u0 - A u, p = r,
+ * rro = r.r, then the persistent loop. */
+int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
+                                  int max_iters, double* p, double* r, double* u,
+                                  const double* u0, double* w, const double* kx,
+                                  const double* ky, int* steps) {
+  double* up[2] = {u, p};
+  int rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 1);
+  if (rc != TL_OK) return rc;
+  rc = launch_map(ctx, ResidualOp{x, y, hd, u, u0, kx, ky, r}, x, y);
+  if (rc != TL_OK) return rc;
+  rc = launch_map(ctx, CopyUOp{x, y, hd, r, p}, x, y);
+  if (rc != TL_OK) return rc;
+  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up + 1, 1);
+  if (rc != TL_OK) return rc;
+  double rro = 0.0;
+  rc = launch_reduce(ctx, Norm2Op{r}, x, y, hd, &rro);
+  if (rc != TL_OK) return rc;
+  return tl_internal_cg64_loop(ctx, x, y, hd, eps, max_iters, p, r, u, w, kx, ky, rro, nullptr,
+                               nullptr, steps);
+}
+
+/* cg_init_driver of TeaLeaf/drivers/cg_driver.c:31-66 on the device:
+ * initialisation kernels, halos of u and p, u0 = u; returns r.p. */
+int tl_internal_cg_setup(tl_context* ctx, int x, int y, int hd, int coefficient, double rx,
+                         double ry, double* p, double* r, double* u, double* u0, double* w,
+                         double* kx, double* ky, const double* density, const double* energy,
+                         double* rro) {
+  *rro = 0.0;
+  int rc = cg_init_impl(ctx, x, y, hd, coefficient, rx, ry, p, r, u, w, kx, ky, density,
+                        energy, rro);
+  if (rc != TL_OK) return rc;
+  double* up[2] = {u, p};
+  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
+  if (rc != TL_OK) return rc;
+  return launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
+}
+
+extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficient,
+                           double rx, double ry, double eps, int max_iters, double* p,
+                           double* r, double* u, double* u0, double* w, double* kx,
+                           double* ky, const double* density, const double* energy,
+                           double* rro0, double* pw_hist, double* rrn_hist, int* steps) {
+  CTX_OK(ctx);
+  DIMS_OK(x, y, hd);
+  TL_REQUIRE(rro0 && steps && (max_iters == 0 || (pw_hist && rrn_hist)),
+             "null output of tl_cg_solve");
+  TL_REQUIRE(max_iters >= 0, "negative max_iters");
+  *steps = 0;
+  double rro = 0.0;
+  int rc = tl_internal_cg_setup(ctx, x, y, hd, coefficient, rx, ry, p, r, u, u0, w, kx, ky,
+                                density, energy, &rro);
+  if (rc != TL_OK) return rc;
+  *rro0 += rro;
+  return tl_internal_cg64_loop(ctx, x, y, hd, eps, max_iters, p, r, u, w, kx, ky, rro,
+                               pw_hist, rrn_hist, steps);
 }
 
 /* ====================================== allocation-free cg_calc_w variant

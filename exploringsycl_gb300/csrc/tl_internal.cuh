@@ -71,6 +71,10 @@ struct tl_context {
   double* d_hist = nullptr;       /* 2 x hist_cap doubles of per-step scalars */
   size_t hist_cap = 0;
   double* d_stage = nullptr;      /* halo pack staging */
+  double* d_diag = nullptr;       /* operator diagonal of the current solve */
+  float* d_f32 = nullptr;         /* mixed-precision solver fields (8 x f32_cap) */
+  size_t f32_cap = 0;
+  size_t diag_cap = 0;
   size_t stage_cap = 0;
   long long launches = 0;
   cudaEvent_t ev_start = nullptr;  /* around the persistent kernel of a solve */
@@ -84,6 +88,21 @@ int tl_cuda_error(cudaError_t e, const char* what, const char* file, int line);
 int tl_ensure_partials(tl_context* ctx, size_t ntiles);
 int tl_ensure_history(tl_context* ctx, size_t n);
 int tl_ensure_stage(tl_context* ctx, size_t n);
+int tl_ensure_diag(tl_context* ctx, size_t n);
+
+/* Internal entry points of tl_fp64.cu shared with the other solvers. */
+int tl_internal_cg_setup(tl_context* ctx, int x, int y, int hd, int coefficient, double rx,
+                         double ry, double* p, double* r, double* u, double* u0, double* w,
+                         double* kx, double* ky, const double* density, const double* energy,
+                         double* rro);
+int tl_internal_cg64_loop(tl_context* ctx, int x, int y, int hd, double eps, int max_iters,
+                          double* p, double* r, double* u, double* w, const double* kx,
+                          const double* ky, double rro, double* pw_hist, double* rrn_hist,
+                          int* steps);
+int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
+                                  int max_iters, double* p, double* r, double* u,
+                                  const double* u0, double* w, const double* kx,
+                                  const double* ky, int* steps);
 
 #define TL_CUDA(call)                                                      \
   do {                                                                     \

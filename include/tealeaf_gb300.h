@@ -211,6 +211,47 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
                 const double* energy, double* rro0, double* pw_hist,
                 double* rrn_hist, int* steps);
 
+/* ------------------------------------------- solver-replacement modes
+ * Whole-timestep solves with a relative FP64 true-residual stop rule, for
+ * the solver-replacement modes of the run_* layer (no counterpart in the
+ * reference, which only has the absolute recurrence-residual rule of
+ * TeaLeaf/drivers/cg_driver.c:24). Each starts as the reference's
+ * cg_init_driver (u = energy*density, kx, ky, halos, u0 = u) and solves
+ * A u = u0 until ||u0 - A u||_2 <= rel_tol ||u0||_2 over the interior,
+ * measured with the exact FP64 kernels. */
+#define TL_METHOD_CG64 0          /* exact FP64 CG (the drop-in kernel) */
+#define TL_METHOD_MIXED_CG 1      /* FP32 inner CG inside FP64 iterative refinement */
+#define TL_METHOD_MIXED_JACOBI 2  /* as above, Jacobi-preconditioned inner CG */
+
+typedef struct tl_solve_params {
+  int method;           /* TL_METHOD_* */
+  double rel_tol;       /* relative FP64 true-residual target */
+  double inner_tol;     /* residual reduction asked of each inner FP32 solve */
+  int max_inner;        /* inner CG steps per outer step (CG64: total steps) */
+  int max_outer;        /* refinement steps */
+  double stall_factor;  /* an outer step must shrink the residual below
+                           stall_factor x the previous one, else FP64 CG
+                           finishes the solve from the current iterate */
+  int max_fallback;     /* FP64 CG steps allowed to the fall-back */
+} tl_solve_params;
+
+typedef struct tl_solve_report {
+  int outer_steps;
+  int inner_steps;
+  int fallback_events;
+  int fallback_steps;
+  double initial_rel_residual;
+  double final_rel_residual;  /* ||u0 - A u|| / ||u0|| in FP64 at return */
+  float device_ms;            /* whole solve, CUDA events on the context stream */
+  float inner_kernel_ms;      /* the persistent inner / CG64 kernels alone */
+} tl_solve_report;
+
+int tl_solve(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
+             double rx, double ry, const tl_solve_params* params, double* p,
+             double* r, double* u, double* u0, double* w, double* kx,
+             double* ky, const double* density, const double* energy,
+             tl_solve_report* report);
+
 /* Device timing of the most recent solve on this context: the persistent
  * kernel alone, measured with CUDA events recorded on the context's stream
  * around its launch, and the number of solver steps it executed. */

@@ -163,9 +163,10 @@ class OracleChunk:
         dt = self.deck.initial_timestep
         return dt / (self.dx * self.dx), dt / (self.dy * self.dy)
 
-    def cg_timestep(self, max_iters=None):
+    def cg_timestep(self, max_iters=None, rel_tol=None):
         """One timestep of the reference CG driver; returns the number of
-        main steps executed and records pw/rrn of each."""
+        main steps executed and records pw/rrn of each. With rel_tol the stop
+        rule becomes sqrt(rr) < rel_tol * ||u0||_2 instead of eps."""
         L, x, y, hd = self.L, self.x, self.y, self.hd
         max_iters = self.deck.max_iters if max_iters is None else max_iters
         rx, ry = self.rx_ry()
@@ -179,6 +180,11 @@ class OracleChunk:
         self.rro0 = rro.value
         self.halos(["u", "p"], 1)
         L.orc_copy_u(x, y, hd, self.p("u"), self.p("u0"))
+        eps = self.deck.eps
+        if rel_tol is not None:
+            bb = C.c_double(0.0)
+            L.orc_calculate_2norm(x, y, hd, self.p("u0"), _pd(bb))
+            eps = rel_tol * np.sqrt(bb.value)
         self.pw_hist, self.rrn_hist = [], []
         rro_v = rro.value
         steps = 0
@@ -197,7 +203,7 @@ class OracleChunk:
             rro_v = rrn.value
             steps = tt + 1
             self.halos(["u", "p"], 1)
-            if np.sqrt(abs(rrn.value)) < self.deck.eps:
+            if np.sqrt(abs(rrn.value)) < eps:
                 break
         self.last_steps = steps
         self.solve_finished()

@@ -3,6 +3,9 @@ backend under the same driver: identical output, bit for bit, for every
 solver; and the tabulated final temperatures of the reference."""
 from __future__ import annotations
 
+import json
+from pathlib import Path
+
 import pytest
 
 from exploringsycl_gb300 import DRIVER_EXE
@@ -41,3 +44,48 @@ def test_tabulated_temperature(n, steps, tmp_path, backend_built):
     run = run_driver(DRIVER_EXE, dk.five_state(n, end_step=steps), tmp_path)
     assert run.returncode == 0, run.stdout[-2000:]
     assert run.passed is True, run.stdout[-800:]
+
+
+@pytest.mark.parametrize("solver", ["cg64", "mixed", "mixed-jacobi"])
+def test_solver_replacement_under_the_driver(solver, tmp_path, backend_built, oracle_built):
+    """gb300_solver in the deck: the driver loop ends after one pass, the
+    backend reports the true solve, and the final temperature agrees with
+    the oracle's plain CG (absolute eps 1e-15) to 1e-8."""
+    d = dk.two_state(96, end_step=2)
+    d.extra = [f"gb300_solver {solver}", "gb300_rel_tol 1e-11"]
+    gpu = run_driver(DRIVER_EXE, d, tmp_path / "gpu")
+    cpu = run_driver(oracle_built.DRIVER, d, tmp_path / "cpu")
+    assert gpu.returncode == 0, gpu.stdout[-2000:]
+    assert gpu.iterations == [0, 0]
+    assert gpu.stdout.count("TL_SOLVE") == 2
+    for line in gpu.stdout.splitlines():
+        if line.startswith("TL_SOLVE"):
+            assert float(line.split("rel_residual=")[1].split()[0]) <= 1e-11
+    tg, tc = gpu.summaries[-1][3], cpu.summaries[-1][3]
+    assert abs(tg - tc) <= 1e-8 * abs(tc)
+
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "reference_driver_runs.json").read_text())
+
+
+class _TextDeck:
+    def __init__(self, text):
+        self._t = text
+
+    def write(self, path):
+        Path(path).write_text(self._t)
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN["runs"] if not n.startswith(("cheby", "ppcg"))])
+def test_gpu_driver_matches_reference_driver_golden(name, tmp_path, backend_built):
+    """The GB300 backend under this project's driver prints exactly what the
+    reference's own driver printed with the oracle kernels: CG step counts,
+    per-step errors and full-precision field summaries, bit for bit. Includes
+    the 256^2 two-state deck of 10 steps (the CPU-vs-GPU summary case)."""
+    g = GOLDEN["runs"][name]
+    r = run_driver(DRIVER_EXE, _TextDeck(g["deck"]), tmp_path)
+    assert r.returncode == 0, r.stdout[-1000:]
+    assert r.iterations == g["iterations"]
+    assert r.errors == g["errors"]
+    assert [list(s) for s in r.summaries] == g["summaries"]
+    assert r.passed == g["passed"]

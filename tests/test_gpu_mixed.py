@@ -1,0 +1,98 @@
+"""Solver-replacement methods on the GPU: each reaches the relative FP64
+true-residual target; the exact FP64 method equals the oracle's CG with the
+same stop rule bit for bit; the mixed-precision methods agree with it to the
+accuracy the target implies; a stalled refinement falls back to FP64 CG.
+
+Tolerance for the mixed methods: both solutions satisfy
+||u0 - A u|| <= 1e-10 ||u0||, so they differ by at most about
+cond(A) * 2e-10 relative; the decks here have cond(A) below 1e3, and the
+tests ask for 1e-7 relative agreement of the temperature and of u."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from exploringsycl_gb300 import deck as dk
+
+pytestmark = pytest.mark.gpu
+
+DECKS = {
+    "two_state_128": lambda: dk.two_state(128, end_step=1),
+    "five_state_96": lambda: dk.five_state(96, end_step=1),
+    "random_160": lambda: dk.random_deck(160, seed=5, end_step=1),
+    "random_odd_75x90": lambda: dk.Deck(75, 90, dk.random_states(8), end_step=1),
+}
+REL = 1e-10
+
+
+def _run(name, method, oracle_built, **kw):
+    from exploringsycl_gb300.chunk import GpuChunk
+    d = DECKS[name]()
+    g = GpuChunk(d)
+    c = oracle_built.OracleChunk(d)
+    try:
+        rep = g.solve_timestep(method, rel_tol=REL, **kw)
+        steps = c.cg_timestep(rel_tol=REL)
+        return g, c, rep, steps
+    except Exception:
+        g.close()
+        raise
+
+
+@pytest.mark.parametrize("name", list(DECKS))
+def test_cg64_method_is_bitwise_oracle_cg(name, backend_built, oracle_built):
+    g, c, rep, steps = _run(name, "cg64", oracle_built)
+    try:
+        assert rep["inner_steps"] == steps
+        assert rep["final_rel_residual"] <= REL
+        assert np.array_equal(g.read("u").view(np.uint64), c.f["u"].view(np.uint64))
+        assert g.summary() == c.summary()
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("name", list(DECKS))
+@pytest.mark.parametrize("method", ["mixed", "mixed-jacobi"])
+def test_mixed_methods_reach_target_and_agree(name, method, backend_built, oracle_built):
+    g, c, rep, steps = _run(name, method, oracle_built)
+    try:
+        assert rep["final_rel_residual"] <= REL, rep
+        assert rep["fallback_events"] == 0, rep
+        assert rep["outer_steps"] >= 2
+        ug, uc = g.read("u"), c.f["u"]
+        hd = g.hd
+        ug = ug.reshape(g.y, g.x)[hd:-hd, hd:-hd]
+        uc = uc.reshape(c.y, c.x)[hd:-hd, hd:-hd]
+        assert np.max(np.abs(ug - uc)) <= 1e-7 * np.max(np.abs(uc))
+        tg, tc = g.summary()[3], c.summary()[3]
+        assert abs(tg - tc) <= 1e-7 * abs(tc)
+    finally:
+        g.close()
+
+
+def test_jacobi_needs_fewer_inner_steps_on_contrasting_densities(backend_built, oracle_built):
+    from exploringsycl_gb300.chunk import GpuChunk
+    d = dk.random_deck(192, seed=2, end_step=1)
+    plain, jac = GpuChunk(d), GpuChunk(d)
+    try:
+        a = plain.solve_timestep("mixed", rel_tol=REL)
+        b = jac.solve_timestep("mixed-jacobi", rel_tol=REL)
+        assert a["final_rel_residual"] <= REL and b["final_rel_residual"] <= REL
+        assert b["inner_steps"] < a["inner_steps"]
+    finally:
+        plain.close()
+        jac.close()
+
+
+def test_stalled_refinement_falls_back_to_fp64_cg(backend_built, oracle_built):
+    """A stall threshold no outer step can meet forces the fall-back after the
+    first refinement step; the FP64 CG then finishes to the target."""
+    g, c, rep, steps = _run("random_160", "mixed", oracle_built, stall_factor=1e-300)
+    try:
+        assert rep["fallback_events"] == 1
+        assert rep["fallback_steps"] > 0
+        assert rep["final_rel_residual"] <= REL
+        tg, tc = g.summary()[3], c.summary()[3]
+        assert abs(tg - tc) <= 1e-7 * abs(tc)
+    finally:
+        g.close()
