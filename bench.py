@@ -56,6 +56,9 @@ BYTES_PER_CELL_STEP = 104          # calc_w 32 + calc_ur 48 + calc_p 24 (FP64)
 # phase 2 reads p_new, w, e, r and writes e, r (24 B); Jacobi adds inv_diag
 # reads in both phases (8 B).
 INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
+# Learned FPCG step: the 8 convolution layers move 2 x 32 B per pixel for each
+# 16-channel activation they read and write, plus the FP32 vectors of FPCG.
+LEARNED_BYTES = 6 * 64 + 2 * 34 + 9 * 4 * 6
 FP64_OPS_PER_CELL_STEP = 19        # FP64 instructions per cell of the exact CG step
 # dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
 # each persistent kernel, from one ncu capture (profiles/*.txt).
@@ -154,7 +157,10 @@ def config_for(args, steps_per_timestep=None) -> dict:
     solver = {"plain": "plain FP64 CG, persistent kernel (run-ahead drop-in)",
               "cg64": "plain FP64 CG, persistent kernel",
               "mixed": "FP32 inner CG in FP64 iterative refinement",
-              "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement"}[args.solver]
+              "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement",
+              "mixed-learned": "FP32 inner flexible PCG with the learned preconditioner "
+                               "(BF16 tensor-core convolutions) in FP64 iterative refinement",
+              }[args.solver]
     return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "
                         f"{stop_rule(args.solver)}, consecutive timesteps",
             "cells": args.size * args.size, "halo_depth": 2, "dt": 0.004,
@@ -269,6 +275,11 @@ class Stepper:
         self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
         self.ctx = ctx
         self.inner_tol = args.inner_tol
+        self.net = None
+        if solver == "mixed-learned":
+            from exploringsycl_gb300.learned import Net, load_weights
+            w, _ = load_weights()
+            self.net = Net(ctx, w)
 
     def step(self) -> dict:
         """Runs one timestep; returns the dominant kernel's time and steps."""
@@ -276,7 +287,8 @@ class Stepper:
             steps = self.chunk.cg_timestep()
             st = self.ctx.solve_stats()
             return {"kernel_ms": st.kernel_ms, "kernel_steps": steps, "cg_steps": steps}
-        rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL, inner_tol=self.inner_tol)
+        rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL, inner_tol=self.inner_tol,
+                                        learned=self.net)
         return {"kernel_ms": rep["inner_kernel_ms"],
                 "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
                 "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
@@ -376,6 +388,8 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     peaks = load_peaks()
     if args.solver in ("plain", "cg64"):
         kernel, bpc = "cg_persistent_kernel", BYTES_PER_CELL_STEP
+    elif args.solver == "mixed-learned":
+        kernel, bpc = "fpcg_learned_step", LEARNED_BYTES
     else:
         kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
     achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9
@@ -441,7 +455,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--deck", choices=["random", "two-state"], default="random")
-    ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "cg64", "plain"],
+    ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned", "cg64", "plain"],
                     default="mixed-jacobi")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
     ap.add_argument("--no-compare", dest="compare", action="store_false",

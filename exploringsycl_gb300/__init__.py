@@ -39,7 +39,7 @@ class TLSolveStats(C.Structure):
 class TLSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("rel_tol", C.c_double), ("inner_tol", C.c_double),
                 ("max_inner", C.c_int), ("max_outer", C.c_int), ("stall_factor", C.c_double),
-                ("max_fallback", C.c_int)]
+                ("max_fallback", C.c_int), ("learned", C.c_void_p)]
 
 
 class TLSolveReport(C.Structure):
@@ -52,8 +52,9 @@ class TLSolveReport(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
-METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI = 0, 1, 2
-METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI}
+METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI, METHOD_MIXED_LEARNED = 0, 1, 2, 3
+METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI,
+           "mixed-learned": METHOD_MIXED_LEARNED}
 
 
 class TLState(C.Structure):
@@ -113,6 +114,20 @@ CONTEXT_FREE = {
     "tl_cg_calc_w_noalloc": [_P, _I, _I, _I, _P, _P, _P, _P, _PD],
 }
 
+# Entry points whose first argument is a network or context handle (prepended).
+HANDLE_FIRST = {
+    "tl_net_create": [C.POINTER(C.c_void_p)],
+    "tl_net_destroy": [],
+    "tl_net_set_weights": [C.POINTER(C.c_float), _I],
+    "tl_net_get_weights": [C.POINTER(C.c_float), _I],
+    "tl_net_apply": [_I, _I, _I, _P, _P, _P],
+    "tl_net_loss_grad": [_I, _I, _I, _I, _P, _P, _P, _P, _PD, C.POINTER(C.c_float)],
+    "tl_net_adam_step": [C.c_float],
+    "tl_net_gather_crops": [_P, _I, _I, C.POINTER(C.c_int), _I, _I, _I, _P],
+    "tl_pack_interior": [_I, _I, _I, _P, _D, _P],
+    "tl_pack_coefficients": [_I, _I, _I, _P, _P, _P, _P, _P],
+}
+
 _lib = None
 
 
@@ -133,10 +148,16 @@ def load_library(path: Path | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = _I
+    for name, args in HANDLE_FIRST.items():
+        fn = getattr(lib, name)
+        fn.argtypes = [_P, *args]
+        fn.restype = _I
     lib.tl_last_error.argtypes = []
     lib.tl_last_error.restype = C.c_char_p
     lib.tl_launch_count.argtypes = [_P]
     lib.tl_launch_count.restype = C.c_longlong
+    lib.tl_net_num_params.argtypes = []
+    lib.tl_net_num_params.restype = _I
     _lib = lib
     return lib
 
@@ -170,6 +191,21 @@ class Context:
         check(self.lib.tl_field_alloc(self.h, n, C.byref(p)), "tl_field_alloc")
         self._fields.append(p.value)
         return p.value
+
+    def alloc_f32(self, n: int) -> int:
+        """Zeroed device array of n floats (allocated as doubles)."""
+        return self.alloc((n + 1) // 2)
+
+    def download_f32(self, dev: int, n: int) -> np.ndarray:
+        out = np.empty((n + 1) // 2, dtype=np.float64)
+        check(self.lib.tl_copy_to_host(self.h, out.ctypes.data, dev, out.size), "download")
+        return out.view(np.float32)[:n].copy()
+
+    def upload_f32(self, dev: int, host: np.ndarray) -> None:
+        a = np.ascontiguousarray(host, dtype=np.float32).ravel()
+        if a.size % 2:
+            a = np.concatenate([a, np.zeros(1, np.float32)])
+        check(self.lib.tl_copy_to_device(self.h, dev, a.ctypes.data, a.size // 2), "upload")
 
     def upload(self, dev: int, host: np.ndarray) -> None:
         a = np.ascontiguousarray(host, dtype=np.float64)

@@ -114,14 +114,17 @@ class GpuChunk:
 
     def solve_timestep(self, method: str = "mixed", rel_tol: float = 1e-10,
                        inner_tol: float = 1e-5, max_inner: int = 20000, max_outer: int = 12,
-                       stall_factor: float = 0.5, max_fallback: int = 20000) -> dict:
+                       stall_factor: float = 0.5, max_fallback: int = 20000,
+                       learned=None) -> dict:
         """One timestep solved to a relative FP64 true residual with one of
-        the solver-replacement methods (cg64 | mixed | mixed-jacobi)."""
+        the solver-replacement methods (cg64 | mixed | mixed-jacobi |
+        mixed-learned, the last with `learned`, a learned.Net)."""
         x, y, hd, f = self.x, self.y, self.hd, self.f
         rx, ry = self.rx_ry()
         self.halos(["energy", "density"], 2)
         prm = TLSolveParams(METHODS[method], rel_tol, inner_tol, max_inner, max_outer,
-                            stall_factor, max_fallback)
+                            stall_factor, max_fallback,
+                            learned.h if learned is not None else None)
         rep = TLSolveReport()
         self.call("tl_solve", x, y, hd, self.coefficient, rx, ry, C.byref(prm), f["p"], f["r"],
                   f["u"], f["u0"], f["w"], f["kx"], f["ky"], f["density"], f["energy"],

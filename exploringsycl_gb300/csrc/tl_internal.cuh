@@ -99,6 +99,12 @@ int tl_internal_cg64_loop(tl_context* ctx, int x, int y, int hd, double eps, int
                           double* p, double* r, double* u, double* w, const double* kx,
                           const double* ky, double rro, double* pw_hist, double* rrn_hist,
                           int* steps);
+struct tl_net;
+int tl_internal_unpack_add(tl_context* ctx, int x, int y, int hd, const float* e,
+                           double inv_scale, double* u);
+int tl_internal_fpcg_learned(tl_context* ctx, tl_net* net, int H, int W, const float* kx,
+                             const float* ky, const float* s, float* r, float* e, float* p,
+                             float* w, float* z, double tol, int max_iters, int* iters);
 int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
                                   int max_iters, double* p, double* r, double* u,
                                   const double* u0, double* w, const double* kx,

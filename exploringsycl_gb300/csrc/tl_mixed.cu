@@ -428,8 +428,14 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     if (rc != TL_OK) return rc;
     rep->final_rel_residual = bnorm > 0 ? rn / bnorm : rn;
   } else {
-    TL_REQUIRE(prm->method == TL_METHOD_MIXED_CG || prm->method == TL_METHOD_MIXED_JACOBI,
+    TL_REQUIRE(prm->method == TL_METHOD_MIXED_CG || prm->method == TL_METHOD_MIXED_JACOBI ||
+                   prm->method == TL_METHOD_MIXED_LEARNED,
                "tl_solve: unknown method");
+    const bool learned = prm->method == TL_METHOD_MIXED_LEARNED;
+    TL_REQUIRE(!learned || prm->learned, "tl_solve: the learned method needs a network");
+    const int H = y - 2 * hd, W = x - 2 * hd;
+    TL_REQUIRE(!learned || (H % 4 == 0 && W % 64 == 0),
+               "tl_solve: the learned preconditioner needs interior sizes H % 4 == 0, W % 64 == 0");
     rc = ensure_mixed(ctx, len);
     if (rc != TL_OK) return rc;
     const size_t ntiles = tl_num_tiles(x, y);
@@ -439,9 +445,15 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     float *kx32 = f, *ky32 = f + len, *invd = f + 2 * (size_t)len, *r32 = f + 3 * (size_t)len,
           *e32 = f + 4 * (size_t)len, *w32 = f + 5 * (size_t)len, *pa = f + 6 * (size_t)len,
           *pb = f + 7 * (size_t)len;
-    coeff_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, kx, ky, kx32, ky32,
-                                                              invd);
-    TL_CHECK_LAUNCH(ctx);
+    if (learned) {
+      /* packed layout: kx32, ky32, invd hold the packed kx, ky, s */
+      rc = tl_pack_coefficients(ctx, x, y, hd, kx, ky, kx32, ky32, invd);
+      if (rc != TL_OK) return rc;
+    } else {
+      coeff_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, kx, ky, kx32, ky32,
+                                                                invd);
+      TL_CHECK_LAUNCH(ctx);
+    }
     const bool vec = (x % 4) == 0;
     const void* kernel = vec ? (const void*)inner_cg_kernel<true> : (const void*)inner_cg_kernel<false>;
     int per_sm = 0;
@@ -480,6 +492,34 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
       }
       prev = rn;
       const double scale = sqrt((double)(x - 2 * hd) * (double)(y - 2 * hd)) / rn;
+      if (learned) {
+        const double need = 0.5 * target / rn;
+        const double tol = std::max(prm->inner_tol, std::min(need, 0.5));
+        rc = tl_pack_interior(ctx, x, y, hd, r, scale, r32);
+        if (rc != TL_OK) return rc;
+        int it = 0;
+        TL_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+        rc = tl_internal_fpcg_learned(ctx, prm->learned, H, W, kx32, ky32, invd, r32, e32, pa,
+                                      w32, pb, tol, prm->max_inner, &it);
+        if (rc != TL_OK) return rc;
+        TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+        TL_CUDA(cudaStreamSynchronize(ctx->stream));
+        /* A broken-down inner solve (non-finite residual) contributes no
+         * correction; the next outer step then sees no progress and falls
+         * back to FP64 CG. */
+        const double rr_in = ((volatile double*)ctx->h_result)[7];
+        if (rr_in == rr_in && rr_in < 1e300) {
+          rc = tl_internal_unpack_add(ctx, x, y, hd, e32, 1.0 / scale, u);
+          if (rc != TL_OK) return rc;
+        }
+        TL_CUDA(cudaStreamSynchronize(ctx->stream));
+        float kms = 0.0f;
+        TL_CUDA(cudaEventElapsedTime(&kms, ctx->ev_start, ctx->ev_stop));
+        rep->inner_kernel_ms += kms;
+        rep->inner_steps += it;
+        rep->outer_steps = outer + 1;
+        continue;
+      }
       demote_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, r, scale, r32, e32,
                                                                   pa, pb);
       TL_CHECK_LAUNCH(ctx);
@@ -509,14 +549,17 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
                                           ctx->stream));
       TL_CHECK_LAUNCH(ctx);
       TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
-      promote_add_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, e32,
-                                                                       1.0 / scale, u);
-      TL_CHECK_LAUNCH(ctx);
       int status = 0;
       TL_CUDA(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
                               ctx->stream));
       TL_CUDA(cudaStreamSynchronize(ctx->stream));
       if (status != 0) return tl_set_error(status, "inner CG kernel: grid-barrier timeout");
+      const double rr_in = ((volatile double*)ctx->h_result)[0];
+      if (rr_in == rr_in && rr_in < 1e300) {
+        promote_add_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, e32,
+                                                                         1.0 / scale, u);
+        TL_CHECK_LAUNCH(ctx);
+      }
       rep->inner_steps += ((volatile int*)ctx->h_steps)[0];
       float kms = 0.0f;
       TL_CUDA(cudaEventElapsedTime(&kms, ctx->ev_start, ctx->ev_stop));

@@ -222,6 +222,8 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
 #define TL_METHOD_CG64 0          /* exact FP64 CG (the drop-in kernel) */
 #define TL_METHOD_MIXED_CG 1      /* FP32 inner CG inside FP64 iterative refinement */
 #define TL_METHOD_MIXED_JACOBI 2  /* as above, Jacobi-preconditioned inner CG */
+#define TL_METHOD_MIXED_LEARNED 3 /* as above, inner flexible PCG with the learned
+                                     preconditioner (params->learned) */
 
 typedef struct tl_solve_params {
   int method;           /* TL_METHOD_* */
@@ -233,6 +235,7 @@ typedef struct tl_solve_params {
                            stall_factor x the previous one, else FP64 CG
                            finishes the solve from the current iterate */
   int max_fallback;     /* FP64 CG steps allowed to the fall-back */
+  struct tl_net* learned; /* TL_METHOD_MIXED_LEARNED: the network, else NULL */
 } tl_solve_params;
 
 typedef struct tl_solve_report {
@@ -251,6 +254,44 @@ int tl_solve(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
              double* r, double* u, double* u0, double* w, double* kx,
              double* ky, const double* density, const double* energy,
              tl_solve_report* report);
+
+/* ----------------------------------------- learned preconditioner
+ * M^-1 = D^-1 + S C^T C S: S = diag(D^-1/2) from the local operator diagonal, C four
+ * bias-free 3x3 convolutions (1 -> 16 -> 16 -> 16 -> 16 channels), BF16
+ * weights and activations, FP32 accumulation (tensor cores for 16 -> 16).
+ * No counterpart in the reference. Arrays are device FP32 [batch][H][W] with
+ * H % 4 == 0 and W % 64 == 0. The weight vector (tl_net_num_params() floats)
+ * is layer 1 [tap][co] (144) then layers 2..4 [tap][ci][co] (2304 each),
+ * tap = 3*(dy+1) + (dx+1) for input offset (dy, dx). */
+typedef struct tl_net tl_net;
+int tl_net_num_params(void);
+int tl_net_create(tl_context* ctx, tl_net** out);
+int tl_net_destroy(tl_net* net);
+int tl_net_set_weights(tl_net* net, const float* host_weights, int n);
+int tl_net_get_weights(tl_net* net, float* host_weights, int n);
+/* z = M^-1 r for B images (s = D^-1/2 per cell). */
+int tl_net_apply(tl_net* net, int H, int W, int B, const float* r, const float* s,
+                 float* z);
+/* Training loss sum_b sum (A z - r)^2 / sum_b sum r^2 over cells at least
+ * `margin` from the image edge, z = M^-1 r, A the 5-point operator with
+ * coupling kx[p] (to the left neighbour) and ky[p] (to the one below);
+ * leaves dL/dweights on the device (and in grad_host if not NULL). */
+int tl_net_loss_grad(tl_net* net, int H, int W, int B, int margin, const float* r,
+                     const float* s, const float* kx, const float* ky, double* loss,
+                     float* grad_host);
+/* One Adam step (beta1 0.9, beta2 0.999) with the last gradients. */
+int tl_net_adam_step(tl_net* net, float lr);
+/* out[b] = crop of data[meta[3b]] at rows meta[3b+1].., columns meta[3b+2]..
+ * (data: device [P][HS][WS]; meta: host int triples). */
+int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, int WS,
+                        const int* meta, int B, int H, int W, float* out);
+/* Interior of a field (x*y with halos) to a packed FP32 [H][W] array times
+ * scale; and the packed FP32 coefficients with s = D^-1/2. */
+int tl_pack_interior(tl_context* ctx, int x, int y, int halo_depth,
+                     const double* field, double scale, float* packed);
+int tl_pack_coefficients(tl_context* ctx, int x, int y, int halo_depth,
+                         const double* kx, const double* ky, float* kx_packed,
+                         float* ky_packed, float* s_packed);
 
 /* Device timing of the most recent solve on this context: the persistent
  * kernel alone, measured with CUDA events recorded on the context's stream

@@ -1,0 +1,51 @@
+"""CPU: the network oracle's hand-written gradient against central finite
+differences (float64), and the symmetry of M^-1 = S C^T C S."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import nn_oracle as nn
+
+
+def _problem(seed=0, B=2, H=12, W=16):
+    rng = np.random.default_rng(seed)
+    r = rng.standard_normal((B, H, W))
+    s = rng.uniform(0.3, 1.0, (B, H, W))
+    kx = rng.uniform(0.1, 3.0, (B, H, W))
+    ky = rng.uniform(0.1, 3.0, (B, H, W))
+    w = rng.standard_normal(9 * 16 + 3 * 9 * 16 * 16) * 0.2
+    return w, r, s, kx, ky
+
+
+def test_gradient_matches_finite_differences():
+    w, r, s, kx, ky = _problem()
+    loss, g = nn.loss_and_grad(w, r, s, kx, ky, margin=2)
+    assert np.isclose(loss, nn.loss_only(w, r, s, kx, ky, 2))
+    rng = np.random.default_rng(1)
+    for _ in range(4):
+        d = rng.standard_normal(w.size)
+        d /= np.linalg.norm(d)
+        h = 1e-5
+        fd = (nn.loss_only(w + h * d, r, s, kx, ky, 2) -
+              nn.loss_only(w - h * d, r, s, kx, ky, 2)) / (2 * h)
+        assert np.isclose(fd, g @ d, rtol=1e-6, atol=1e-9), (fd, g @ d)
+
+
+def test_preconditioner_is_symmetric():
+    w, r, s, _, _ = _problem(3)
+    r2 = np.random.default_rng(4).standard_normal(r.shape)
+    a = np.sum(nn.forward(w, r, s) * r2)
+    b = np.sum(r * nn.forward(w, r2, s))
+    assert np.isclose(a, b, rtol=1e-12)
+    assert np.sum(nn.forward(w, r, s) * r) >= 0.0
+
+
+def test_identity_weights_are_jacobi():
+    """With C = identity-like weights (C^T C = I) M^-1 = 2 D^-1, and with
+    C = 0 the Jacobi term alone remains: M^-1 = D^-1."""
+    from exploringsycl_gb300.learned import identity_weights
+    _, r, s, _, _ = _problem(5)
+    z = nn.forward(identity_weights().astype(np.float64), r, s)
+    assert np.allclose(z, 2 * s * s * r)
+    z0 = nn.forward(np.zeros(identity_weights().size), r, s)
+    assert np.allclose(z0, s * s * r)
