@@ -275,6 +275,8 @@ class Stepper:
         self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
         self.ctx = ctx
         self.inner_tol = args.inner_tol
+        self.max_inner = args.max_inner
+        self.max_outer = args.max_outer
         self.net = None
         if solver == "mixed-learned":
             from exploringsycl_gb300.learned import Net, load_weights
@@ -288,7 +290,8 @@ class Stepper:
             st = self.ctx.solve_stats()
             return {"kernel_ms": st.kernel_ms, "kernel_steps": steps, "cg_steps": steps}
         rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL, inner_tol=self.inner_tol,
-                                        learned=self.net)
+                                        learned=self.net, max_inner=self.max_inner,
+                                        max_outer=self.max_outer)
         return {"kernel_ms": rep["inner_kernel_ms"],
                 "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
                 "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
@@ -458,6 +461,9 @@ def main() -> None:
     ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned", "cg64", "plain"],
                     default="mixed-jacobi")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--max-inner", type=int, default=20000,
+                    help="inner steps per refinement step (smaller only for profiling captures)")
+    ap.add_argument("--max-outer", type=int, default=12)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the plain FP64 CG run of the same timesteps")
     ap.add_argument("--e2e-steps", type=int, default=2)

@@ -112,6 +112,7 @@ CONTEXT_FREE = {
     "tl_copy_to_host": [_P, _P, _P, C.c_size_t],
     "tl_last_solve_stats": [_P, C.POINTER(TLSolveStats)],
     "tl_cg_calc_w_noalloc": [_P, _I, _I, _I, _P, _P, _P, _P, _PD],
+    "tl_selftest_barrier_timeout": [_P, _I, _PI],
 }
 
 # Entry points whose first argument is a network or context handle (prepended).

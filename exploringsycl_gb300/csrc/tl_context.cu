@@ -209,3 +209,28 @@ extern "C" int tl_copy_to_host(tl_context* ctx, double* host, const double* dev,
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
   return TL_OK;
 }
+
+/* One block waits at the grid barrier for an arrival that never comes
+ * (expected = 2 with a single block), for budget_ms; the barrier gives up,
+ * records TL_ERR_TIMEOUT and the kernel returns. */
+static __global__ void barrier_selftest_kernel(unsigned* sync, int* status,
+                                               unsigned long long budget_ns) {
+  tl_grid_barrier_n(sync, status, 2u, budget_ns);
+}
+
+extern "C" int tl_selftest_barrier_timeout(tl_context* ctx, int budget_ms, int* status) {
+  TL_REQUIRE(ctx && status && budget_ms > 0 && budget_ms <= 1000,
+             "tl_selftest_barrier_timeout: budget must be in (0, 1000] ms");
+  TL_CUDA(cudaMemsetAsync(ctx->d_sync + TL_SYNC_BAR_COUNT, 0, 2 * sizeof(unsigned), ctx->stream));
+  TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  barrier_selftest_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_sync, ctx->d_status,
+                                                     (unsigned long long)budget_ms * 1000000ull);
+  TL_CHECK_LAUNCH(ctx);
+  TL_CUDA(cudaMemcpyAsync(status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  /* leave the barrier words clean for the next persistent kernel */
+  TL_CUDA(cudaMemsetAsync(ctx->d_sync + TL_SYNC_BAR_COUNT, 0, 2 * sizeof(unsigned), ctx->stream));
+  TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  return TL_OK;
+}

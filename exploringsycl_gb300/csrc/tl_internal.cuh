@@ -195,12 +195,14 @@ __device__ __forceinline__ unsigned long long tl_globaltimer() {
   return t;
 }
 
-/* Grid-wide barrier for co-resident blocks (cooperative launch). Spins for
- * at most TL_BARRIER_BUDGET_NS; on expiry it records TL_ERR_TIMEOUT in
- * *status and returns false instead of waiting further. Returns false as
- * well when any block has recorded an error, so that all blocks leave their
- * loops together. */
-__device__ __forceinline__ bool tl_grid_barrier(unsigned* sync, int* status) {
+/* Grid-wide barrier for co-resident blocks (cooperative launch): waits until
+ * `expected` blocks have arrived. Spins for at most `budget_ns` of
+ * %globaltimer; on expiry it records TL_ERR_TIMEOUT in *status and returns
+ * false instead of waiting further. Returns false as well when any block has
+ * recorded an error, so that all blocks leave their loops together. */
+__device__ __forceinline__ bool tl_grid_barrier_n(unsigned* sync, int* status,
+                                                  unsigned expected,
+                                                  unsigned long long budget_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -209,14 +211,14 @@ __device__ __forceinline__ bool tl_grid_barrier(unsigned* sync, int* status) {
     const unsigned my_gen = *gen;
     __threadfence();
     const unsigned arrived = atomicAdd(sync + TL_SYNC_BAR_COUNT, 1u);
-    if (arrived == gridDim.x - 1) {
+    if (arrived == expected - 1) {
       atomicExch(sync + TL_SYNC_BAR_COUNT, 0u);
       __threadfence();
       atomicAdd(sync + TL_SYNC_BAR_GEN, 1u);
     } else {
       const unsigned long long t0 = tl_globaltimer();
       while (*gen == my_gen) {
-        if (tl_globaltimer() - t0 > TL_BARRIER_BUDGET_NS) {
+        if (tl_globaltimer() - t0 > budget_ns) {
           atomicCAS(status, 0, TL_ERR_TIMEOUT);
           ok = 0;
           break;
@@ -230,4 +232,8 @@ __device__ __forceinline__ bool tl_grid_barrier(unsigned* sync, int* status) {
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool tl_grid_barrier(unsigned* sync, int* status) {
+  return tl_grid_barrier_n(sync, status, gridDim.x, TL_BARRIER_BUDGET_NS);
 }

@@ -28,8 +28,10 @@
  *      visited in reverse order so that the most recently written tiles of
  *      phase 1 are still in L2.
  * Memory per cell and step: 24 B + 24 B (+ 8 B with Jacobi) in FP32, against
- * 104 B for the FP64 step. Partial sums are FP32 within a tile and FP64
- * across tiles, reduced in a fixed order (deterministic).
+ * 104 B for the FP64 step. Each thread keeps its partial sums in FP32
+ * registers across all of its block's tiles; one block reduction per phase
+ * gives one FP64 partial per block, and the partials are reduced in a fixed
+ * order by every block (deterministic, no per-tile synchronisation).
  */
 #include <math.h>
 #include <stdio.h>
@@ -105,9 +107,9 @@ __global__ void __launch_bounds__(kThreads, 1) inner_cg_kernel(InnerParams P, in
 
     if (k > 0) {
       /* ---- phase 1: p_new = z + beta p_old, w = A p_new, p.w */
+      float pw = 0.0f;
       for (int tile = blockIdx.x; tile < P.ntiles; tile += G) {
         const unsigned i0 = (unsigned)tile * TL_TILE + 4u * threadIdx.x;
-        float pw = 0.0f;
         if (kVec) {
           const int jj = (int)(i0 / (unsigned)x);
           const int kk0 = (int)(i0 - (unsigned)jj * (unsigned)x);
@@ -207,20 +209,23 @@ __global__ void __launch_bounds__(kThreads, 1) inner_cg_kernel(InnerParams P, in
             w[i] = wq;
           }
         }
+      }
+      {
         const float t = block_sum_f(pw, s_warp[0]);
-        if (threadIdx.x == 0) P.part_pw[tile] = (double)t;
+        if (threadIdx.x == 0) P.part_pw[blockIdx.x] = (double)t;
       }
       if (!tl_grid_barrier(P.sync, P.status)) break;
-      const double pwsum = tl_reduce_partials(P.part_pw, P.ntiles, s_scratch);
+      const double pwsum = tl_reduce_partials(P.part_pw, G, s_scratch);
       const double alpha = rz_old / pwsum;
       const float af = (float)alpha;
 
       /* ---- phase 2: e += alpha p, r -= alpha w, r.r and r.z (reverse order) */
       const int count = (P.ntiles - 1 - blockIdx.x) / G + 1;
+      float rr = 0.0f, rz = 0.0f;
+#pragma unroll 2
       for (int c = count - 1; c >= 0; --c) {
         const int tile = blockIdx.x + c * G;
         const unsigned i0 = (unsigned)tile * TL_TILE + 4u * threadIdx.x;
-        float rr = 0.0f, rz = 0.0f;
         if (i0 < len) {
           if (kVec) {
             const float4 pp = __ldcg(reinterpret_cast<const float4*>(pnew + i0));
@@ -231,10 +236,10 @@ __global__ void __launch_bounds__(kThreads, 1) inner_cg_kernel(InnerParams P, in
             rv.x -= af * ww.x; rv.y -= af * ww.y; rv.z -= af * ww.z; rv.w -= af * ww.w;
             *reinterpret_cast<float4*>(e + i0) = ee;
             *reinterpret_cast<float4*>(r + i0) = rv;
-            rr = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+            rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
             if (P.jacobi) {
               const float4 d = __ldg(reinterpret_cast<const float4*>(P.invd + i0));
-              rz = rv.x * rv.x * d.x + rv.y * rv.y * d.y + rv.z * rv.z * d.z + rv.w * rv.w * d.w;
+              rz += rv.x * rv.x * d.x + rv.y * rv.y * d.y + rv.z * rv.z * d.z + rv.w * rv.w * d.w;
             }
           } else {
 #pragma unroll
@@ -250,19 +255,19 @@ __global__ void __launch_bounds__(kThreads, 1) inner_cg_kernel(InnerParams P, in
             }
           }
         }
-        /* Cells outside the interior hold r = 0 and contribute nothing. */
-        const float t1 = block_sum_f(rr, s_warp[1]);
-        const float t2 = P.jacobi ? block_sum_f(rz, s_warp[2]) : t1;
-        if (threadIdx.x == 0) {
-          P.part_rr[tile] = (double)t1;
-          P.part_rz[tile] = (double)t2;
-        }
+      }
+      /* Cells outside the interior hold r = 0 and contribute nothing. */
+      const float t1 = block_sum_f(rr, s_warp[1]);
+      const float t2 = P.jacobi ? block_sum_f(rz, s_warp[2]) : t1;
+      if (threadIdx.x == 0) {
+        P.part_rr[blockIdx.x] = (double)t1;
+        P.part_rz[blockIdx.x] = (double)t2;
       }
     } else {
       /* ---- step 0: r.r and r.z of the incoming residual */
+      float rr = 0.0f, rz = 0.0f;
       for (int tile = blockIdx.x; tile < P.ntiles; tile += G) {
         const unsigned i0 = (unsigned)tile * TL_TILE + 4u * threadIdx.x;
-        float rr = 0.0f, rz = 0.0f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const unsigned i = i0 + q;
@@ -271,17 +276,17 @@ __global__ void __launch_bounds__(kThreads, 1) inner_cg_kernel(InnerParams P, in
           rr += rv * rv;
           if (P.jacobi) rz += rv * rv * __ldg(P.invd + i);
         }
-        const float t1 = block_sum_f(rr, s_warp[1]);
-        const float t2 = P.jacobi ? block_sum_f(rz, s_warp[2]) : t1;
-        if (threadIdx.x == 0) {
-          P.part_rr[tile] = (double)t1;
-          P.part_rz[tile] = (double)t2;
-        }
+      }
+      const float t1 = block_sum_f(rr, s_warp[1]);
+      const float t2 = P.jacobi ? block_sum_f(rz, s_warp[2]) : t1;
+      if (threadIdx.x == 0) {
+        P.part_rr[blockIdx.x] = (double)t1;
+        P.part_rz[blockIdx.x] = (double)t2;
       }
     }
     if (!tl_grid_barrier(P.sync, P.status)) break;
-    const double rr = tl_reduce_partials(P.part_rr, P.ntiles, s_scratch);
-    const double rz = P.jacobi ? tl_reduce_partials(P.part_rz, P.ntiles, s_scratch) : rr;
+    const double rr = tl_reduce_partials(P.part_rr, G, s_scratch);
+    const double rz = P.jacobi ? tl_reduce_partials(P.part_rz, G, s_scratch) : rr;
     if (k == 0) {
       rr0 = rr;
       beta = 0.0;

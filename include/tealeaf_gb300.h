@@ -351,6 +351,15 @@ int tl_ppcg_inner_iteration(tl_context* ctx, int x, int y, int halo_depth,
                             double* sd, double* r, double* u,
                             const double* kx, const double* ky);
 
+/* ---------------------------------------------------- failure detection
+ * Self-test of the bounded grid-barrier wait used by every persistent
+ * kernel: a single block waits for a second arrival that never comes, gives
+ * up after budget_ms (at most 1000) and records TL_ERR_TIMEOUT, which is
+ * returned in *status; the context stays usable. No counterpart in the
+ * reference (its host waits are unbounded, TeaLeaf/c_kernels/sycl/
+ * sycl_shared.hpp:358). */
+int tl_selftest_barrier_timeout(tl_context* ctx, int budget_ms, int* status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,39 @@
+"""Failure detection without a GPU fault: a bounded in-kernel wait runs out
+and reports TL_ERR_TIMEOUT, after which the same context still solves
+correctly; bad arguments are refused before any launch."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from exploringsycl_gb300 import TLError
+from exploringsycl_gb300 import deck as dk
+
+pytestmark = pytest.mark.gpu
+
+
+def test_barrier_wait_times_out_and_context_survives(backend_built, oracle_built):
+    from exploringsycl_gb300.chunk import GpuChunk
+    g = GpuChunk(dk.five_state(32, end_step=1))
+    try:
+        status = C.c_int(-1)
+        g.call("tl_selftest_barrier_timeout", 50, C.byref(status))
+        assert status.value == 3  # TL_ERR_TIMEOUT
+        c = oracle_built.OracleChunk(g.deck)
+        assert g.cg_timestep() == c.cg_timestep()
+        assert g.summary() == c.summary()
+    finally:
+        g.close()
+
+
+def test_invalid_arguments_are_refused(backend_built):
+    from exploringsycl_gb300 import Context
+    with Context(0) as ctx:
+        pw = C.c_double(0.0)
+        with pytest.raises(TLError):   # empty interior
+            ctx.call("tl_cg_calc_w", 4, 4, 2, None, None, None, None, C.byref(pw))
+        status = C.c_int(0)
+        with pytest.raises(TLError):   # budget above one second
+            ctx.call("tl_selftest_barrier_timeout", 5000, C.byref(status))
