@@ -64,7 +64,7 @@ FP64_OPS_PER_CELL_STEP = 19        # FP64 instructions per cell of the exact CG 
 # each persistent kernel, from one ncu capture (profiles/*.txt).
 NCU_BYTES_PER_CELL_STEP = {
     "cg_persistent_kernel": 112.3,  # profiles/cg_persistent_fp64_4096.txt (104 + diag 8)
-    "inner_cg_kernel": None,
+    "inner_cg_kernel": 51.3,        # profiles/inner_cg_mixed_jacobi_4096.txt
 }
 ITER_FIXTURES = {"two-state": ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json",
                  "random": ROOT / "tests" / "golden" / "cg_iterations_random_4096.json"}

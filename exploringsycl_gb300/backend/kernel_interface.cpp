@@ -42,14 +42,18 @@
  * Environment: TL_DEVICE (GPU index, default 0), TL_CG_MODE ("fused", the
  * default, or "stepwise"), TL_SOLVER (as gb300_solver), TL_PRINT_SUMMARY=1
  * (print the four field-summary sums at full precision), TL_PRINT_SOLVE=1
- * (print per-solve device steps).
+ * (print per-solve device steps), TL_DUMP_DIR=<dir> (write density, energy
+ * and u as VisIt BOV files at every field summary).
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #include "kernel_interface.h"
 #include "tealeaf_gb300.h"
+#include "../host/tl_dump.h" /* header-only field dump */
 
 #define TL_TRY(call, what)                                                     \
   do {                                                                         \
@@ -267,6 +271,22 @@ void run_field_summary(Chunk* chunk, Settings* settings, double* vol,
          "field_summary");
   if (env_is("TL_PRINT_SUMMARY", "1")) {
     printf("TL_SUMMARY %.17e %.17e %.17e %.17e\n", *vol, *mass, *ie, *temp);
+  }
+  const char* dump = getenv("TL_DUMP_DIR");
+  if (dump && *dump) {
+    /* density, energy and u of every field summary, numbered in order */
+    static int dump_count = 0;
+    std::vector<double> host((size_t)chunk->x * chunk->y);
+    const struct { const char* name; double* f; } fields[] = {
+        {"density", chunk->density}, {"energy", chunk->energy}, {"u", chunk->u}};
+    for (const auto& fd : fields) {
+      TL_TRY(tl_copy_to_host(chunk->ext->ctx, host.data(), fd.f, host.size()), "dump copy");
+      if (tl_dump_interior(dump, fd.name, dump_count, 0.0, chunk->x, chunk->y,
+                           settings->halo_depth, host.data()) != 0) {
+        die(__LINE__, __FILE__, "GB300 backend: cannot write dumps to %s\n", dump);
+      }
+    }
+    dump_count++;
   }
   STOP_PROFILING(settings->kernel_profile, __func__);
 }

@@ -15,6 +15,7 @@
 #include <stdlib.h>
 
 #include "kernel_interface.h"
+#include "../../exploringsycl_gb300/host/tl_dump.h" /* header-only field dump */
 #include "tl_oracle.h"
 
 static double* alloc_zeroed(size_t n) {
@@ -153,6 +154,19 @@ void run_field_summary(Chunk* chunk, Settings* settings, double* vol,
   const char* env = getenv("TL_PRINT_SUMMARY");
   if (env && env[0] == '1') {
     printf("TL_SUMMARY %.17e %.17e %.17e %.17e\n", *vol, *mass, *ie, *temp);
+  }
+  const char* dump = getenv("TL_DUMP_DIR");
+  if (dump && *dump) {
+    static int dump_count = 0;
+    const struct { const char* name; double* f; } fields[] = {
+        {"density", chunk->density}, {"energy", chunk->energy}, {"u", chunk->u}};
+    for (const auto& fd : fields) {
+      if (tl_dump_interior(dump, fd.name, dump_count, 0.0, chunk->x, chunk->y,
+                           settings->halo_depth, fd.f) != 0) {
+        die(__LINE__, __FILE__, "oracle backend: cannot write dumps to %s\n", dump);
+      }
+    }
+    dump_count++;
   }
   STOP_PROFILING(settings->kernel_profile, __func__);
 }
