@@ -56,9 +56,10 @@ BYTES_PER_CELL_STEP = 104          # calc_w 32 + calc_ur 48 + calc_p 24 (FP64)
 # phase 2 reads p_new, w, e, r and writes e, r (24 B); Jacobi adds inv_diag
 # reads in both phases (8 B).
 INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
-# Learned FPCG step: the 8 convolution layers move 2 x 32 B per pixel for each
-# 16-channel activation they read and write, plus the FP32 vectors of FPCG.
-LEARNED_BYTES = 6 * 64 + 2 * 34 + 9 * 4 * 6
+# Learned FPCG step (collapsed stencil, one persistent kernel): phase P reads
+# z, p_old, kx, ky and writes p_new, w (24 B); phase Z reads r, w, s, p_new, e
+# and writes r, e, z (32 B).
+LEARNED_BYTES = 56
 FP64_OPS_PER_CELL_STEP = 19        # FP64 instructions per cell of the exact CG step
 # dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
 # each persistent kernel, from one ncu capture (profiles/*.txt).
@@ -159,7 +160,8 @@ def config_for(args, steps_per_timestep=None) -> dict:
               "mixed": "FP32 inner CG in FP64 iterative refinement",
               "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement",
               "mixed-learned": "FP32 inner flexible PCG with the learned preconditioner "
-                               "(BF16 tensor-core convolutions) in FP64 iterative refinement",
+                               "(network collapsed to a 17x17 stencil on the tensor cores) "
+                               "in FP64 iterative refinement",
               }[args.solver]
     return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "
                         f"{stop_rule(args.solver)}, consecutive timesteps",
@@ -392,7 +394,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     if args.solver in ("plain", "cg64"):
         kernel, bpc = "cg_persistent_kernel", BYTES_PER_CELL_STEP
     elif args.solver == "mixed-learned":
-        kernel, bpc = "fpcg_learned_step", LEARNED_BYTES
+        kernel, bpc = "lpcg_kernel", LEARNED_BYTES
     else:
         kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
     achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9

@@ -53,8 +53,10 @@ class TLSolveReport(C.Structure):
 
 
 METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI, METHOD_MIXED_LEARNED = 0, 1, 2, 3
+METHOD_MIXED_LEARNED_LAYERS = 4
 METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI,
-           "mixed-learned": METHOD_MIXED_LEARNED}
+           "mixed-learned": METHOD_MIXED_LEARNED,
+           "mixed-learned-layers": METHOD_MIXED_LEARNED_LAYERS}
 
 
 class TLState(C.Structure):
@@ -124,6 +126,8 @@ HANDLE_FIRST = {
     "tl_net_apply": [_I, _I, _I, _P, _P, _P],
     "tl_net_loss_grad": [_I, _I, _I, _I, _P, _P, _P, _P, _PD, C.POINTER(C.c_float)],
     "tl_net_adam_step": [C.c_float],
+    "tl_net_stencil": [C.POINTER(C.c_float), C.POINTER(C.c_float)],
+    "tl_net_apply_stencil": [_I, _I, _P, _P, _P],
     "tl_net_gather_crops": [_P, _I, _I, C.POINTER(C.c_int), _I, _I, _I, _P],
     "tl_pack_interior": [_I, _I, _I, _P, _D, _P],
     "tl_pack_coefficients": [_I, _I, _I, _P, _P, _P, _P, _P],

@@ -118,7 +118,9 @@ class GpuChunk:
                        learned=None) -> dict:
         """One timestep solved to a relative FP64 true residual with one of
         the solver-replacement methods (cg64 | mixed | mixed-jacobi |
-        mixed-learned, the last with `learned`, a learned.Net)."""
+        mixed-learned | mixed-learned-layers, the last two with `learned`, a
+        learned.Net: its collapsed stencil in one persistent kernel, or the
+        network applied layer by layer)."""
         x, y, hd, f = self.x, self.y, self.hd, self.f
         rx, ry = self.rx_ry()
         self.halos(["energy", "density"], 2)

@@ -105,6 +105,16 @@ int tl_internal_unpack_add(tl_context* ctx, int x, int y, int hd, const float* e
 int tl_internal_fpcg_learned(tl_context* ctx, tl_net* net, int H, int W, const float* kx,
                              const float* ky, const float* s, float* r, float* e, float* p,
                              float* w, float* z, double tol, int max_iters, int* iters);
+/* The learned preconditioner collapsed to one stencil (tl_precond.cu). */
+int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
+                            const float** kscale);
+int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
+                                int W, const float* r, const float* s, float* z);
+int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* kscale, int H,
+                               int W, const float* kx, const float* ky, const float* s,
+                               float* r, float* r_alt, float* e, float* w, float* z, float* pa,
+                               float* pb, double tol, int max_iters, int* iters,
+                               double* rr_final);
 int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
                                   int max_iters, double* p, double* r, double* u,
                                   const double* u0, double* w, const double* kx,

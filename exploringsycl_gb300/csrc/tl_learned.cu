@@ -41,6 +41,7 @@
 #include <stdio.h>
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
@@ -468,6 +469,107 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
   w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+/* ----------------------------------------------- collapse to a stencil */
+
+constexpr int kStencil = 17;            /* C^T C: 17 x 17 taps */
+constexpr int kFragEntries = 17 * 2 * 2 * 32;
+constexpr int kUmmaHalves = 17 * 2 * 256;  /* 34 B operands of 16 x 16 FP16 */
+
+/* Composes the four layers into the 16-channel 9x9 kernel G of C (G(u)
+ * multiplies the input at offset u), then K(d) = sum_u G(u).G(u + d), the
+ * stencil of C^T C, and the tensor-core B fragments of its banded Toeplitz
+ * blocks (tl_precond.cu): entry [dy][par][kb][lane] holds
+ * T(k, n) = K(dy, 16 kb + k - 8 - 8 par - n) for k = 2t, 2t+1 and 2t+8, 2t+9,
+ * n = g (lane = 4 g + t), as FP16 pairs, K scaled by kscale = 2^-ceil(log2 max|K|).
+ * umma holds the same Toeplitz blocks as tcgen05 B operands: matrix
+ * (dy, kb) at halves 256 (2 dy + kb), element (n, k) = T(k, n) at
+ * (k / 8) 128 + 8 n + k % 8 (K-major core matrices, 16 x 16).
+ * One block; runs whenever the weights change. */
+__global__ void __launch_bounds__(256) collapse_kernel(const float* __restrict__ master,
+                                                        float* __restrict__ k_out,
+                                                        uint2* __restrict__ frag,
+                                                        __half* __restrict__ umma,
+                                                        float* __restrict__ kscale_out) {
+  __shared__ float s_g[2][81 * kCh];
+  __shared__ float s_k[kStencil * kStencil];
+  __shared__ float s_max[8];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 81 * kCh; i += blockDim.x) {
+    const int u = i / kCh, c = i % kCh;
+    const int uy = u / 9 - 4, ux = u % 9 - 4;
+    float v = 0.0f;
+    if (uy >= -1 && uy <= 1 && ux >= -1 && ux <= 1) v = master[(3 * (uy + 1) + ux + 1) * kCh + c];
+    s_g[0][i] = v;
+  }
+  __syncthreads();
+  int cur = 0;
+  for (int l = 0; l < 3; ++l) {
+    const float* wl = master + 9 * kCh + l * 9 * kCh * kCh;  /* [tap][ci][co] */
+    for (int i = tid; i < 81 * kCh; i += blockDim.x) {
+      const int u = i / kCh, co = i % kCh;
+      const int uy = u / 9 - 4, ux = u % 9 - 4;
+      float acc = 0.0f;
+      for (int tap = 0; tap < 9; ++tap) {
+        const int vy = uy - (tap / 3 - 1), vx = ux - (tap % 3 - 1);
+        if (vy < -4 || vy > 4 || vx < -4 || vx > 4) continue;
+        const float* gv = &s_g[cur][((vy + 4) * 9 + vx + 4) * kCh];
+        for (int ci = 0; ci < kCh; ++ci) acc += gv[ci] * wl[(tap * kCh + ci) * kCh + co];
+      }
+      s_g[cur ^ 1][i] = acc;
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  const float* gk = s_g[cur];
+  float local_max = 0.0f;
+  for (int d = tid; d < kStencil * kStencil; d += blockDim.x) {
+    const int dy = d / kStencil - 8, dx = d % kStencil - 8;
+    float acc = 0.0f;
+    for (int uy = -4; uy <= 4; ++uy) {
+      const int vy = uy + dy;
+      if (vy < -4 || vy > 4) continue;
+      for (int ux = -4; ux <= 4; ++ux) {
+        const int vx = ux + dx;
+        if (vx < -4 || vx > 4) continue;
+        const float* a = &gk[((uy + 4) * 9 + ux + 4) * kCh];
+        const float* b = &gk[((vy + 4) * 9 + vx + 4) * kCh];
+        for (int c = 0; c < kCh; ++c) acc += a[c] * b[c];
+      }
+    }
+    s_k[d] = acc;
+    k_out[d] = acc;
+    local_max = fmaxf(local_max, fabsf(acc));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(TL_FULL_MASK, local_max, o));
+  if ((tid & 31) == 0) s_max[tid >> 5] = local_max;
+  __syncthreads();
+  float kmax = 0.0f;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) kmax = fmaxf(kmax, s_max[i]);
+  const float kscale = kmax > 0.0f ? exp2f(-ceilf(log2f(kmax))) : 1.0f;
+  if (tid == 0) *kscale_out = kscale;
+  auto tap = [&](int dy, int dx) -> float {
+    return (dx < -8 || dx > 8) ? 0.0f : kscale * s_k[(dy + 8) * kStencil + dx + 8];
+  };
+  for (int i = tid; i < kFragEntries; i += blockDim.x) {
+    const int lane = i & 31, kb = (i >> 5) & 1, par = (i >> 6) & 1, dyi = i >> 7;
+    const int g = lane >> 2, t = lane & 3, dy = dyi - 8;
+    const int base = 16 * kb - 8 - 8 * par - g;
+    const __half2 lo = __floats2half2_rn(tap(dy, base + 2 * t), tap(dy, base + 2 * t + 1));
+    const __half2 hi = __floats2half2_rn(tap(dy, base + 2 * t + 8), tap(dy, base + 2 * t + 9));
+    uint2 v;
+    v.x = *reinterpret_cast<const uint32_t*>(&lo);
+    v.y = *reinterpret_cast<const uint32_t*>(&hi);
+    frag[i] = v;
+  }
+  for (int i = tid; i < kUmmaHalves; i += blockDim.x) {
+    const int mat = i >> 8, e = i & 255;
+    const int dyi = mat >> 1, kb = mat & 1;
+    const int k = (e >> 7) * 8 + (e & 7), n = (e >> 3) & 15;
+    umma[i] = __float2half_rn(tap(dyi - 8, 16 * kb + k - 8 - n));
+  }
+}
+
 }  // namespace
 
 /* ============================================================== network */
@@ -500,6 +602,11 @@ struct tl_net {
   float* dadj = nullptr;
   double* sums = nullptr;
   int sums_cap = 0;
+  /* the network collapsed to its 17x17 stencil (collapse_kernel) */
+  float* stencil_k = nullptr;     /* K, 289 floats */
+  uint2* stencil_frag = nullptr;  /* tensor-core fragments of K * kscale (FP16) */
+  __half* stencil_umma = nullptr; /* the same as tcgen05 B operands */
+  float* stencil_kscale = nullptr;
 };
 
 static int net_param_count() { return 9 * kCh + 3 * 9 * kCh * kCh; }
@@ -634,6 +741,10 @@ __global__ void to_bf16_kernel(const float* __restrict__ a, __nv_bfloat16* __res
 static int refresh_weights(tl_net* net) {
   make_weights_kernel<<<(3 * 9 * kCh * kCh + 255) / 256, 256, 0, net->ctx->stream>>>(
       net->master, net->fwd16, net->adj16, net->l1_fwd, net->l1_adj);
+  TL_CHECK_LAUNCH(net->ctx);
+  collapse_kernel<<<1, 256, 0, net->ctx->stream>>>(net->master, net->stencil_k,
+                                                    net->stencil_frag, net->stencil_umma,
+                                                    net->stencil_kscale);
   TL_CHECK_LAUNCH(net->ctx);
   return TL_OK;
 }
@@ -911,6 +1022,10 @@ extern "C" int tl_net_create(tl_context* ctx, tl_net** out) {
   if (e == cudaSuccess) e = cudaMalloc(&net->l1_fwd, 9 * kCh * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&net->l1_adj, 9 * kCh * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&net->dadj, n16 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_k, kStencil * kStencil * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_frag, kFragEntries * sizeof(uint2));
+  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_umma, kUmmaHalves * sizeof(__half));
+  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_kscale, sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(net->master, 0, np * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(net->adam_m, 0, np * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(net->adam_v, 0, np * sizeof(float));
@@ -928,6 +1043,8 @@ extern "C" int tl_net_destroy(tl_net* net) {
   cudaFree(net->master); cudaFree(net->grad); cudaFree(net->adam_m); cudaFree(net->adam_v);
   cudaFree(net->fwd16); cudaFree(net->adj16); cudaFree(net->l1_fwd); cudaFree(net->l1_adj);
   cudaFree(net->dadj); cudaFree(net->partial);
+  cudaFree(net->stencil_k); cudaFree(net->stencil_frag); cudaFree(net->stencil_kscale);
+  cudaFree(net->stencil_umma);
   for (auto& a : net->act) cudaFree(a);
   for (auto& a : net->bct) cudaFree(a);
   cudaFree(net->b0); cudaFree(net->q); cudaFree(net->gz); cudaFree(net->g16a);
@@ -990,6 +1107,34 @@ extern "C" int tl_net_loss_grad(tl_net* net, int H, int W, int B, int margin, co
                             cudaMemcpyDeviceToHost, net->ctx->stream));
     TL_CUDA(cudaStreamSynchronize(net->ctx->stream));
   }
+  return TL_OK;
+}
+
+extern "C" int tl_net_stencil(tl_net* net, float* host_k, float* kscale) {
+  TL_REQUIRE(net && host_k, "tl_net_stencil: null argument");
+  TL_CUDA(cudaMemcpyAsync(host_k, net->stencil_k, kStencil * kStencil * sizeof(float),
+                          cudaMemcpyDeviceToHost, net->ctx->stream));
+  float ks = 0.0f;
+  TL_CUDA(cudaMemcpyAsync(&ks, net->stencil_kscale, sizeof(float), cudaMemcpyDeviceToHost,
+                          net->ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(net->ctx->stream));
+  if (kscale) *kscale = ks;
+  return TL_OK;
+}
+
+extern "C" int tl_net_apply_stencil(tl_net* net, int H, int W, const float* r, const float* s,
+                                    float* z) {
+  TL_REQUIRE(net && r && s && z, "tl_net_apply_stencil: null argument");
+  return tl_internal_apply_collapsed(net->ctx, net->stencil_umma, net->stencil_kscale, H, W, r,
+                                     s, z);
+}
+
+int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
+                            const float** kscale) {
+  TL_REQUIRE(net && frag && umma && kscale, "tl_internal_net_stencil: null argument");
+  *frag = net->stencil_frag;
+  *umma = net->stencil_umma;
+  *kscale = net->stencil_kscale;
   return TL_OK;
 }
 

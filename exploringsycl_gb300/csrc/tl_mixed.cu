@@ -364,14 +364,17 @@ int grid_for(tl_context* ctx, unsigned len) {
 
 }  // namespace
 
-/* Scratch of the mixed solver: 8 float fields of x*y. */
+/* Scratch of the mixed solvers: kMixedFields float arrays of x*y cells,
+ * each starting on a 256-byte boundary (slot k at d_f32 + k * f32_cap). */
+constexpr int kMixedFields = 10;
 static int ensure_mixed(tl_context* ctx, size_t n) {
+  n = (n + 63) & ~(size_t)63;
   if (n <= ctx->f32_cap) return TL_OK;
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
   cudaFree(ctx->d_f32);
   ctx->d_f32 = nullptr;
   ctx->f32_cap = 0;
-  TL_CUDA(cudaMalloc(&ctx->d_f32, 8 * n * sizeof(float)));
+  TL_CUDA(cudaMalloc(&ctx->d_f32, kMixedFields * n * sizeof(float)));
   ctx->f32_cap = n;
   return TL_OK;
 }
@@ -434,22 +437,27 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     rep->final_rel_residual = bnorm > 0 ? rn / bnorm : rn;
   } else {
     TL_REQUIRE(prm->method == TL_METHOD_MIXED_CG || prm->method == TL_METHOD_MIXED_JACOBI ||
-                   prm->method == TL_METHOD_MIXED_LEARNED,
+                   prm->method == TL_METHOD_MIXED_LEARNED ||
+                   prm->method == TL_METHOD_MIXED_LEARNED_LAYERS,
                "tl_solve: unknown method");
-    const bool learned = prm->method == TL_METHOD_MIXED_LEARNED;
+    const bool layers = prm->method == TL_METHOD_MIXED_LEARNED_LAYERS;
+    const bool learned = layers || prm->method == TL_METHOD_MIXED_LEARNED;
     TL_REQUIRE(!learned || prm->learned, "tl_solve: the learned method needs a network");
     const int H = y - 2 * hd, W = x - 2 * hd;
-    TL_REQUIRE(!learned || (H % 4 == 0 && W % 64 == 0),
-               "tl_solve: the learned preconditioner needs interior sizes H % 4 == 0, W % 64 == 0");
+    TL_REQUIRE(!layers || (H % 4 == 0 && W % 64 == 0),
+               "tl_solve: the layer-by-layer network needs interior sizes H % 4 == 0, W % 64 == 0");
+    TL_REQUIRE(!learned || layers || W % 4 == 0,
+               "tl_solve: the learned preconditioner needs an interior width W % 4 == 0");
     rc = ensure_mixed(ctx, len);
     if (rc != TL_OK) return rc;
     const size_t ntiles = tl_num_tiles(x, y);
     rc = tl_ensure_partials(ctx, ntiles);
     if (rc != TL_OK) return rc;
     float* f = ctx->d_f32;
-    float *kx32 = f, *ky32 = f + len, *invd = f + 2 * (size_t)len, *r32 = f + 3 * (size_t)len,
-          *e32 = f + 4 * (size_t)len, *w32 = f + 5 * (size_t)len, *pa = f + 6 * (size_t)len,
-          *pb = f + 7 * (size_t)len;
+    const size_t cap = ctx->f32_cap;
+    float *kx32 = f, *ky32 = f + cap, *invd = f + 2 * cap, *r32 = f + 3 * cap,
+          *e32 = f + 4 * cap, *w32 = f + 5 * cap, *pa = f + 6 * cap, *pb = f + 7 * cap,
+          *z32 = f + 8 * cap, *r32b = f + 9 * cap;
     if (learned) {
       /* packed layout: kx32, ky32, invd hold the packed kx, ky, s */
       rc = tl_pack_coefficients(ctx, x, y, hd, kx, ky, kx32, ky32, invd);
@@ -503,16 +511,28 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
         rc = tl_pack_interior(ctx, x, y, hd, r, scale, r32);
         if (rc != TL_OK) return rc;
         int it = 0;
+        double rr_in = 0.0;
         TL_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
-        rc = tl_internal_fpcg_learned(ctx, prm->learned, H, W, kx32, ky32, invd, r32, e32, pa,
-                                      w32, pb, tol, prm->max_inner, &it);
+        if (layers) {
+          rc = tl_internal_fpcg_learned(ctx, prm->learned, H, W, kx32, ky32, invd, r32, e32, pa,
+                                        w32, pb, tol, prm->max_inner, &it);
+        } else {
+          const void* frag = nullptr;
+          const void* umma = nullptr;
+          const float* kscale = nullptr;
+          rc = tl_internal_net_stencil(prm->learned, &frag, &umma, &kscale);
+          if (rc != TL_OK) return rc;
+          rc = tl_internal_fpcg_collapsed(ctx, frag, kscale, H, W, kx32, ky32, invd, r32, r32b,
+                                          e32, w32, z32, pa, pb, tol, prm->max_inner, &it,
+                                          &rr_in);
+        }
         if (rc != TL_OK) return rc;
         TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
         TL_CUDA(cudaStreamSynchronize(ctx->stream));
         /* A broken-down inner solve (non-finite residual) contributes no
          * correction; the next outer step then sees no progress and falls
          * back to FP64 CG. */
-        const double rr_in = ((volatile double*)ctx->h_result)[7];
+        if (layers) rr_in = ((volatile double*)ctx->h_result)[7];
         if (rr_in == rr_in && rr_in < 1e300) {
           rc = tl_internal_unpack_add(ctx, x, y, hd, e32, 1.0 / scale, u);
           if (rc != TL_OK) return rc;

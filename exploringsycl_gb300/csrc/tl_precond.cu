@@ -1,0 +1,713 @@
+/*
+ * tl_precond.cu -- the learned preconditioner collapsed to one stencil, and
+ * the persistent flexible-PCG kernel of the mixed-precision solver that
+ * applies it on the tensor cores.
+ *
+ * Collapse. The network of tl_learned.cu has no bias and no activation, so
+ * between its two diagonal scalings it is a linear, translation-invariant
+ * operator: the four 3x3 layers compose to C r = sum_u G(u) r(. + u) with a
+ * 16-channel 9x9 kernel G, and the adjoint stack C^T C is the 17x17 stencil
+ *   K(d) = sum_u G(u) . G(u + d),      z = D^-1 r + S (K * (S r)),
+ * where (K * y)(j) = sum_d K(d) y(j + d). K is the autocorrelation of G:
+ * symmetric, with a non-negative Fourier transform. More than 8 cells from
+ * the domain edge the stencil and the layer-by-layer network are the same
+ * operator (tests check this to rounding); at the edge the stencil acts on
+ * the zero-extended field once instead of truncating every layer, so S K S
+ * is a principal submatrix of a positive semi-definite Toeplitz operator and
+ * M^-1 stays symmetric positive definite. Cost: 289 multiply-adds per cell
+ * against ~28 k for the eight 16-channel layers. K and the fragment table
+ * below are built on the device from the FP32 master weights whenever the
+ * weights change (tl_learned.cu, collapse_kernel).
+ *
+ * Tensor cores. For a block of 16 output rows and one row offset dy, the
+ * correlation along a row with K(dy, .) is a product with a banded Toeplitz
+ * matrix: for 8 output columns starting at xc, the inputs xc-8 .. xc+15 form
+ * two 16-column k-blocks, and
+ *   Z[16 x 8] += Y[16 x 16] T0[16 x 8] + Y'[16 x 16] T1[16 x 8],
+ * T(k, n) = K(dy, 16 kb + k - 8 - 8 par - n) (0 where |dx| > 8), with par the
+ * parity of the 8-column block within its 16-column window. That is 34
+ * mma.sync m16n8k16 (FP16 inputs, FP32 accumulation) per 128 outputs. A warp
+ * owns 16 rows x 32 columns: per dy it loads three 16x16 data windows with
+ * ldmatrix and four T fragments (the same for every tile, kept in shared
+ * memory in fragment order) and issues 8 MMAs. The scaled residual y = S r is
+ * staged in FP16 with its 8-cell halo, multiplied by sigma = 1 / RMS(r) so
+ * that its values sit in FP16's normal range whatever the residual's size
+ * (the operator is linear; the factor is removed in the epilogue); K is
+ * scaled by a power of two for the same reason.
+ *
+ * Flexible PCG (Polak-Ribiere beta = z_new.(r_new - r_old) / z_old.r_old,
+ * r_new - r_old = -alpha w), on the packed interior [H][W] with zero-flux
+ * edges, one cooperative persistent kernel, two phases and two grid barriers
+ * per step:
+ *   P: p_new = z + beta p_old at the cell and its four neighbours, w = A p_new,
+ *      p.w partial sums (linear chunks of 2048 cells, float4 per thread), and
+ *      the previous step's e += alpha p_old;
+ *   Z: r_new = r_old - alpha w and y = sigma S r_new on a 64 x 128 tile and its
+ *      halo (shared memory, FP16), z = S K y / sigma + D^-1 r_new on the tensor
+ *      cores; partial sums of r.r, r.z and z.w.
+ * The residual is double-buffered because a tile reads its neighbours' old
+ * residual while they write the new one. Memory per cell and step: P reads z,
+ * p_old, kx, ky, e and writes p_new, w, e (32 B); Z reads r, w, s and writes r,
+ * z (20 B): 52 B, against 56 B for the Jacobi-PCG kernel of tl_mixed.cu. The
+ * last step's e update is one extra pass at the end. Tiles of phase Z are
+ * visited in reverse order so that the cells phase P wrote last are still in
+ * L2.
+ */
+#include <cuda_fp16.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "tl_internal.cuh"
+#include "tl_tc05.cuh"
+
+namespace {
+
+constexpr int kTH = 64;                 /* phase Z tile rows */
+constexpr int kTW = 64;                 /* phase Z tile columns */
+constexpr int kWarpsX = kTW / 32;       /* a warp owns 16 rows x 32 columns */
+constexpr int kThreads = 32 * kWarpsX * (kTH / 16);
+constexpr int kBlocksPerSM = 4;
+constexpr int kChunk = 4 * kThreads;    /* phase P: cells per block iteration */
+constexpr int kHalo = 8;
+constexpr int kRows = kTH + 2 * kHalo;  /* staged rows */
+constexpr int kCols = kTW + 2 * kHalo;  /* staged columns */
+/* halves per staged row: a multiple of 8 (16-byte ldmatrix rows) whose word
+ * stride is 4 x odd modulo 32, so the 8 rows of an ldmatrix phase fall in
+ * distinct banks */
+constexpr int kStride = kCols + 8;
+static_assert(kStride % 8 == 0 && ((kStride / 2) % 8) == 4, "bank-conflicting row stride");
+constexpr int kFrag = 17 * 2 * 2 * 32;  /* uint2 entries of the Toeplitz fragment table */
+
+struct LpcgParams {
+  int H, W, chunks, tiles_x, tiles, max_iters;
+  double tol2;
+  const float *kx, *ky, *s;
+  float *r0, *r1;  /* residual, double-buffered (r0 holds the incoming one) */
+  float *e, *w, *z, *p0, *p1;
+  const uint2* frag;
+  const float* kscale;
+  double* part;  /* 4 arrays of gridDim.x partial sums */
+  unsigned* sync;
+  int* status;
+  int* iters_out;
+  double* rr_out;
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TL_FULL_MASK, v, o);
+  return v;
+}
+
+/* Block-wide sum in a fixed order; every thread returns it. */
+__device__ __forceinline__ float block_sum(float v, float* s_red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) s_red[warp] = v;
+  __syncthreads();
+  float t = lane < (kThreads / 32) ? s_red[lane] : 0.0f;
+  t = warp_sum(t);
+  __syncthreads();
+  return t;
+}
+
+/* Sum of n doubles written by other blocks before a grid barrier, in one
+ * fixed order (lane-strided sequential sums, then a butterfly), so that
+ * every block obtains the same bits. */
+__device__ __forceinline__ double sum_partials(const double* part, int n, double* s_one) {
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(part + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TL_FULL_MASK, v, o);
+    if (threadIdx.x == 0) *s_one = v;
+  }
+  __syncthreads();
+  const double t = *s_one;
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t a[4], const __half* src) {
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(src);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+               : "r"(addr));
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) {
+  return __ldcg(reinterpret_cast<const float4*>(p));
+}
+__device__ __forceinline__ float2 ld2(const float* p) {
+  return __ldcg(reinterpret_cast<const float2*>(p));
+}
+
+/* Stages y = sigma * s * (r - alpha w) for tile rows y0-8 .. y0+71 and columns
+ * x0-8 .. x0+135 as FP16 (zero outside the domain). W % 4 == 0, so a group of
+ * four columns is entirely inside or outside. w may be null (alpha = 0). Each
+ * thread issues the loads of two groups before it converts and stores them. */
+__device__ __forceinline__ void stage_tile(int H, int W, int y0, int x0, const float* rold,
+                                           const float* w, const float* s, float alpha,
+                                           float sigma, __half* s_y) {
+  constexpr int kGroups = kCols / 4;
+  constexpr int kTotal = kRows * kGroups;
+  for (int q0 = threadIdx.x; q0 < kTotal; q0 += 2 * kThreads) {
+    float4 r[2], ww[2], ss[2];
+    bool in[2];
+    int off[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int q = q0 + u * kThreads;
+      const int row = q / kGroups, grp = q - row * kGroups;
+      const int gy = y0 - kHalo + row, gx = x0 - kHalo + 4 * grp;
+      off[u] = row * kStride + 4 * grp;
+      in[u] = q < kTotal && gy >= 0 && gy < H && gx >= 0 && gx < W;
+      r[u] = ww[u] = ss[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in[u]) {
+        const size_t i = (size_t)gy * W + gx;
+        r[u] = ld4(rold + i);
+        if (w) ww[u] = ld4(w + i);
+        ss[u] = __ldg(reinterpret_cast<const float4*>(s + i));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (q0 + u * kThreads >= kTotal) break;
+      const float4 rv = make_float4(r[u].x - alpha * ww[u].x, r[u].y - alpha * ww[u].y,
+                                    r[u].z - alpha * ww[u].z, r[u].w - alpha * ww[u].w);
+      const __half2 lo = __floats2half2_rn(sigma * ss[u].x * rv.x, sigma * ss[u].y * rv.y);
+      const __half2 hi = __floats2half2_rn(sigma * ss[u].z * rv.z, sigma * ss[u].w * rv.w);
+      uint2 packed;
+      packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+      packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+      *reinterpret_cast<uint2*>(s_y + off[u]) = packed;
+    }
+  }
+}
+
+/* acc[j] = (K * y) for this warp's 16 x 32 block: rows wr.., columns
+ * wc + 8j.., in the m16n8 accumulator layout. */
+__device__ __forceinline__ void stencil_mma(const __half* s_y, const uint2* s_frag, int wr,
+                                            int wc, float acc[4][4]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[j][q] = 0.0f;
+  const __half* base = s_y + (wr + (lane & 15)) * kStride + wc + (lane >> 4) * 8;
+#pragma unroll 1
+  for (int dyi = 0; dyi < 17; ++dyi) {
+    uint32_t a0[4], a1[4];
+    const __half* src = base + dyi * kStride;
+    const uint2* f = s_frag + dyi * 128 + lane;
+    const uint2 b00 = f[0], b01 = f[32], b10 = f[64], b11 = f[96];
+    ldmatrix_x4(a0, src);
+    ldmatrix_x4(a1, src + 16);
+    mma16816(acc[0], a0, b00);
+    mma16816(acc[0], a1, b01);
+    mma16816(acc[1], a0, b10);
+    mma16816(acc[1], a1, b11);
+    ldmatrix_x4(a0, src + 32);
+    mma16816(acc[2], a1, b00);
+    mma16816(acc[2], a0, b01);
+    mma16816(acc[3], a1, b10);
+    mma16816(acc[3], a0, b11);
+  }
+}
+
+__device__ __forceinline__ void load_frag(const uint2* frag, uint2* s_frag) {
+  for (int i = threadIdx.x; i < kFrag; i += kThreads) s_frag[i] = frag[i];
+}
+
+/* ------------------------------------------------------------ phase P */
+
+/* p_new = z + beta p_old, w = A p_new, p.w; and the previous step's
+ * e += alpha_prev p_old (p_old is loaded here anyway). */
+__device__ __forceinline__ float phase_p(const LpcgParams& P, const float* __restrict__ pold,
+                                         float* __restrict__ pnew, float bf, float a_prev) {
+  const int H = P.H, W = P.W;
+  const size_t n = (size_t)H * W;
+  const int lane = threadIdx.x & 31;
+  const float* __restrict__ z = P.z;
+  float pw = 0.0f;
+  for (int c = blockIdx.x; c < P.chunks; c += gridDim.x) {
+    const size_t i0 = (size_t)c * kChunk + 4u * threadIdx.x;
+    const bool act = i0 < n;
+    const int yy = act ? (int)(i0 / (unsigned)W) : 0;
+    const int xx0 = act ? (int)(i0 - (size_t)yy * W) : 0;
+    float4 pc = make_float4(0.f, 0.f, 0.f, 0.f), pu = pc, pd = pc, kxc = pc, kyc = pc,
+           kyu = pc;
+    if (act) {
+      const float4 zc = ld4(z + i0), oc = ld4(pold + i0);
+      float4 ev = ld4(P.e + i0);
+      pc = make_float4(zc.x + bf * oc.x, zc.y + bf * oc.y, zc.z + bf * oc.z, zc.w + bf * oc.w);
+      ev.x += a_prev * oc.x; ev.y += a_prev * oc.y; ev.z += a_prev * oc.z; ev.w += a_prev * oc.w;
+      *reinterpret_cast<float4*>(P.e + i0) = ev;
+      if (yy + 1 < H) {
+        const float4 zu = ld4(z + i0 + W), ou = ld4(pold + i0 + W);
+        pu = make_float4(zu.x + bf * ou.x, zu.y + bf * ou.y, zu.z + bf * ou.z, zu.w + bf * ou.w);
+        kyu = __ldg(reinterpret_cast<const float4*>(P.ky + i0 + W));
+      }
+      if (yy > 0) {
+        const float4 zd = ld4(z + i0 - W), od = ld4(pold + i0 - W);
+        pd = make_float4(zd.x + bf * od.x, zd.y + bf * od.y, zd.z + bf * od.z, zd.w + bf * od.w);
+      }
+      kxc = __ldg(reinterpret_cast<const float4*>(P.kx + i0));
+      kyc = __ldg(reinterpret_cast<const float4*>(P.ky + i0));
+    }
+    float pl = __shfl_up_sync(TL_FULL_MASK, pc.w, 1);
+    float pr = __shfl_down_sync(TL_FULL_MASK, pc.x, 1);
+    float kx4 = __shfl_down_sync(TL_FULL_MASK, kxc.x, 1);
+    if (lane == 0 && act && xx0 > 0) pl = __ldcg(z + i0 - 1) + bf * __ldcg(pold + i0 - 1);
+    if (lane == 31 && act && xx0 + 4 < W) {
+      pr = __ldcg(z + i0 + 4) + bf * __ldcg(pold + i0 + 4);
+      kx4 = __ldg(P.kx + i0 + 4);
+    }
+    if (!act) continue;
+    const float pv[4] = {pc.x, pc.y, pc.z, pc.w};
+    const float pvu[4] = {pu.x, pu.y, pu.z, pu.w};
+    const float pvd[4] = {pd.x, pd.y, pd.z, pd.w};
+    const float kxv[5] = {kxc.x, kxc.y, kxc.z, kxc.w, kx4};
+    const float kyv[4] = {kyc.x, kyc.y, kyc.z, kyc.w};
+    const float kyuv[4] = {kyu.x, kyu.y, kyu.z, kyu.w};
+    float wv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int xx = xx0 + q;
+      const float a = pv[q];
+      const float al = (xx == 0) ? a : (q == 0 ? pl : pv[q - 1]);
+      const float ar = (xx == W - 1) ? a : (q == 3 ? pr : pv[q + 1]);
+      const float ad = (yy == 0) ? a : pvd[q];
+      const float au = (yy == H - 1) ? a : pvu[q];
+      wv[q] = a + kxv[q + 1] * (a - ar) + kxv[q] * (a - al) + kyuv[q] * (a - au) +
+              kyv[q] * (a - ad);
+      pw += wv[q] * a;
+    }
+    *reinterpret_cast<float4*>(pnew + i0) = pc;
+    *reinterpret_cast<float4*>(P.w + i0) = make_float4(wv[0], wv[1], wv[2], wv[3]);
+  }
+  return pw;
+}
+
+/* ------------------------------------------------------------ phase Z */
+
+struct ZSums {
+  float rr, rz, zw;
+};
+
+/* One tile of phase Z. kFused: r_new = r_old - alpha w is written to rnew
+ * and the dot products are accumulated; otherwise (the stand-alone
+ * application) z = M^-1 r only. */
+template <bool kFused>
+__device__ __forceinline__ void phase_z_tile(int H, int W, int tile, int tiles_x,
+                                             const float* __restrict__ rold,
+                                             float* __restrict__ rnew,
+                                             const float* __restrict__ w,
+                                             const float* __restrict__ s,
+                                             float* __restrict__ z,
+                                             float alpha, float sigma, float zscale,
+                                             __half* s_y, const uint2* s_frag, ZSums& sums) {
+  const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+  const int y0 = ty * kTH, x0 = tx * kTW;
+  stage_tile(H, W, y0, x0, rold, kFused ? w : nullptr, s, alpha, sigma, s_y);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wr = (warp / kWarpsX) * 16, wc = (warp % kWarpsX) * 32;
+  float acc[4][4];
+  stencil_mma(s_y, s_frag, wr, wc, acc);
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int gy = y0 + wr + g + 8 * h, gx = x0 + wc + 8 * j + 2 * t;
+      if (gy >= H || gx >= W) continue;
+      const size_t i = (size_t)gy * W + gx;
+      float2 rn = ld2(rold + i);
+      float2 ww = make_float2(0.f, 0.f);
+      if (kFused) {
+        ww = ld2(w + i);
+        rn.x -= alpha * ww.x;
+        rn.y -= alpha * ww.y;
+      }
+      const float2 ss = __ldg(reinterpret_cast<const float2*>(s + i));
+      const float2 zv = make_float2(ss.x * (acc[j][2 * h] * zscale) + ss.x * ss.x * rn.x,
+                                    ss.y * (acc[j][2 * h + 1] * zscale) + ss.y * ss.y * rn.y);
+      *reinterpret_cast<float2*>(z + i) = zv;
+      if (kFused) {
+        *reinterpret_cast<float2*>(rnew + i) = rn;
+        sums.rr += rn.x * rn.x + rn.y * rn.y;
+        sums.rz += rn.x * zv.x + rn.y * zv.y;
+        sums.zw += zv.x * ww.x + zv.y * ww.y;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+/* ----------------------------------------------------- persistent FPCG */
+
+__global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams P) {
+  __shared__ __align__(16) __half s_y[kRows * kStride];
+  __shared__ __align__(16) uint2 s_frag[kFrag];
+  __shared__ float s_red[kThreads / 32];
+  __shared__ double s_one;
+  const int G = gridDim.x;
+  const int H = P.H, W = P.W;
+  const double n = (double)H * (double)W;
+  load_frag(P.frag, s_frag);
+  const float zscale_k = 1.0f / __ldg(P.kscale);
+  double* part_pw = P.part;
+  double* part_rr = P.part + G;
+  double* part_rz = P.part + 2 * G;
+  double* part_zw = P.part + 3 * G;
+
+  /* r.r of the incoming residual: its RMS sets the FP16 staging scale. */
+  {
+    float rr = 0.0f;
+    const size_t total = (size_t)H * W;
+    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < total;
+         i += (size_t)G * kThreads) {
+      const float v = __ldcg(P.r0 + i);
+      rr += v * v;
+    }
+    rr = block_sum(rr, s_red);
+    if (threadIdx.x == 0) part_rr[blockIdx.x] = (double)rr;
+  }
+  if (!tl_grid_barrier(P.sync, P.status)) return;
+  double rr = sum_partials(part_rr, G, &s_one);
+  const double rr0 = rr;
+  double rz_old = 0.0, alpha = 0.0, beta = 0.0;
+  int par_r = 0, par_p = 0, iters = 0;
+  bool done = !(rr0 > 0.0) || P.max_iters <= 0;
+
+  for (int k = 0; !done; ++k) {
+    float* rcur = par_r ? P.r1 : P.r0;
+    float* rnext = par_r ? P.r0 : P.r1;
+    const float* pold = par_p ? P.p1 : P.p0;
+    float* pnew = par_p ? P.p0 : P.p1;
+    if (k > 0) {
+      /* ---- phase P */
+      float pw = phase_p(P, pold, pnew, (float)beta, (float)alpha);
+      pw = block_sum(pw, s_red);
+      if (threadIdx.x == 0) part_pw[blockIdx.x] = (double)pw;
+      if (!tl_grid_barrier(P.sync, P.status)) return;
+      const double pwsum = sum_partials(part_pw, G, &s_one);
+      alpha = rz_old / pwsum;
+    }
+    /* ---- phase Z (step 0: z0 = M^-1 r0, alpha = 0) */
+    const float sigma = (float)(1.0 / sqrt(rr / n));
+    const float zscale = zscale_k / sigma;
+    const float af = (float)alpha;
+    ZSums sums = {0.0f, 0.0f, 0.0f};
+    for (int c = blockIdx.x; c < P.tiles; c += G) {
+      const int tile = P.tiles - 1 - c;
+      phase_z_tile<true>(H, W, tile, P.tiles_x, rcur, rnext, P.w, P.s, P.z, af, sigma, zscale,
+                         s_y, s_frag, sums);
+    }
+    const float t_rr = block_sum(sums.rr, s_red);
+    const float t_rz = block_sum(sums.rz, s_red);
+    const float t_zw = block_sum(sums.zw, s_red);
+    if (threadIdx.x == 0) {
+      part_rr[blockIdx.x] = (double)t_rr;
+      part_rz[blockIdx.x] = (double)t_rz;
+      part_zw[blockIdx.x] = (double)t_zw;
+    }
+    if (!tl_grid_barrier(P.sync, P.status)) return;
+    rr = sum_partials(part_rr, G, &s_one);
+    const double rz = sum_partials(part_rz, G, &s_one);
+    const double zw = sum_partials(part_zw, G, &s_one);
+    beta = (k == 0) ? 0.0 : -alpha * zw / rz_old;
+    rz_old = rz;
+    par_r ^= 1;
+    if (k > 0) par_p ^= 1;
+    iters = k;
+    if (rr <= P.tol2 * rr0 || !(rr == rr) || k >= P.max_iters) done = true;
+  }
+  /* The last step's e += alpha p (every earlier one was added in phase P). */
+  if (iters > 0) {
+    const float* plast = par_p ? P.p1 : P.p0;
+    const float af = (float)alpha;
+    const size_t n4 = (size_t)H * W / 4;
+    for (size_t q = (size_t)blockIdx.x * kThreads + threadIdx.x; q < n4;
+         q += (size_t)G * kThreads) {
+      const float4 pp = ld4(plast + 4 * q);
+      float4 ev = ld4(P.e + 4 * q);
+      ev.x += af * pp.x; ev.y += af * pp.y; ev.z += af * pp.z; ev.w += af * pp.w;
+      *reinterpret_cast<float4*>(P.e + 4 * q) = ev;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *P.iters_out = iters;
+    *P.rr_out = rr;
+  }
+}
+
+/* ------------------------------------------- stand-alone application */
+
+__global__ void rms_partial_kernel(const float* __restrict__ r, size_t n,
+                                   double* __restrict__ part) {
+  __shared__ float s_red[kThreads / 32];
+  float rr = 0.0f;
+  for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * kThreads) {
+    const float v = r[i];
+    rr += v * v;
+  }
+  rr = block_sum(rr, s_red);
+  if (threadIdx.x == 0) part[blockIdx.x] = (double)rr;
+}
+
+/* ------------------------------------ tcgen05 stencil (stand-alone)
+ *
+ * One 128 x 64 tile per block, 8 warps. The scaled residual y is staged in
+ * FP16 as the MMA's A operand: ten K-major chunks of 8 staged columns, each
+ * 144 rows x 16 bytes (+16 bytes of padding so that the stores of one row
+ * spread over the banks). For output columns 16 nb .. 16 nb + 15 and row
+ * offset dy, the two 16-column windows of the band are chunks 2 nb + 2 kb and
+ * 2 nb + 2 kb + 1 (LBO = chunk size), shifted down by dy + 8 rows (16 bytes
+ * per row, SBO = 128); the B operands are the 34 Toeplitz blocks T(dy, kb)
+ * (16 x 16). 136 MMAs of M = 128, N = 16, K = 16 accumulate the tile in 64
+ * tensor-memory columns (lane = tile row); the epilogue reads them back with
+ * tcgen05.ld, one row per thread. */
+constexpr int kUTH = 128;
+constexpr int kUTW = 64;
+constexpr int kUThreads = 256;
+constexpr int kURows = kUTH + 2 * kHalo;
+constexpr int kUChunks = (kUTW + 2 * kHalo) / 8;
+constexpr int kUChunkBytes = kURows * 16 + 16;
+constexpr int kUBBytes = 17 * 2 * 512;
+constexpr uint32_t kUTmemCols = 64;
+constexpr uint32_t kUIdesc = tc05::idesc_f16_f32<128, 16>();
+constexpr unsigned long long kUWaitNs = 1000000000ull;
+
+__global__ void __launch_bounds__(kUThreads) stencil_apply_tc05_kernel(
+    int H, int W, int tiles_x, const float* __restrict__ r, const float* __restrict__ s,
+    float* __restrict__ z, const __half* __restrict__ umma, const float* __restrict__ kscale,
+    const double* __restrict__ part, int nparts, int* __restrict__ status) {
+  __shared__ __align__(1024) unsigned char s_a[kUChunks * kUChunkBytes];
+  __shared__ __align__(1024) unsigned char s_b[kUBBytes];
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  __shared__ double s_one;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    tc05::tmem_alloc(&s_tmem, kUTmemCols);
+    tc05::tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    tc05::mbar_init(&s_mbar, 1);
+    tc05::mbar_fence_init();
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+
+  double rr = 0.0;
+  if (threadIdx.x < 32) {
+    for (int i = threadIdx.x; i < nparts; i += 32) rr += part[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rr += __shfl_xor_sync(TL_FULL_MASK, rr, o);
+    if (threadIdx.x == 0) s_one = rr;
+  }
+  __syncthreads();
+  rr = s_one;
+  const double n = (double)H * (double)W;
+  const float sigma = rr > 0.0 ? (float)(1.0 / sqrt(rr / n)) : 1.0f;
+  const float zscale = 1.0f / (__ldg(kscale) * sigma);
+
+  /* B operands */
+  for (int i = threadIdx.x; i < kUBBytes / 16; i += kUThreads)
+    reinterpret_cast<uint4*>(s_b)[i] = reinterpret_cast<const uint4*>(umma)[i];
+  /* A operand: y = sigma s r, rows y0-8 .., columns x0-8 .., zero outside */
+  const int ty = blockIdx.x / tiles_x, tx = blockIdx.x - ty * tiles_x;
+  const int y0 = ty * kUTH, x0 = tx * kUTW;
+  constexpr int kGroups = (kUTW + 2 * kHalo) / 4;
+  for (int q = threadIdx.x; q < kURows * kGroups; q += kUThreads) {
+    const int row = q / kGroups, grp = q - row * kGroups;
+    const int gy = y0 - kHalo + row, gx = x0 - kHalo + 4 * grp;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+      const size_t i = (size_t)gy * W + gx;
+      const float4 rv = __ldg(reinterpret_cast<const float4*>(r + i));
+      const float4 sv = __ldg(reinterpret_cast<const float4*>(s + i));
+      v = make_float4(sigma * sv.x * rv.x, sigma * sv.y * rv.y, sigma * sv.z * rv.z,
+                      sigma * sv.w * rv.w);
+    }
+    const __half2 lo = __floats2half2_rn(v.x, v.y), hi = __floats2half2_rn(v.z, v.w);
+    uint2 packed;
+    packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+    packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+    *reinterpret_cast<uint2*>(s_a + (grp >> 1) * kUChunkBytes + row * 16 + (grp & 1) * 8) =
+        packed;
+  }
+  tc05::fence_proxy_async_smem();
+  __syncthreads();
+
+  if (threadIdx.x == 0) {
+    tc05::fence_after_sync();
+    const uint32_t a0 = tc05::smem_addr(s_a), b0 = tc05::smem_addr(s_b);
+    for (int nb = 0; nb < kUTW / 16; ++nb) {
+      for (int dyi = 0; dyi < 17; ++dyi) {
+#pragma unroll
+        for (int kb = 0; kb < 2; ++kb) {
+          const uint64_t ad = tc05::smem_desc(a0 + (2 * nb + 2 * kb) * kUChunkBytes + dyi * 16,
+                                              kUChunkBytes, 128);
+          const uint64_t bd = tc05::smem_desc(b0 + (2 * dyi + kb) * 512, 256, 128);
+          tc05::mma_f16(tmem + 16 * nb, ad, bd, kUIdesc, (dyi | kb) != 0);
+        }
+      }
+    }
+    tc05::mma_commit(&s_mbar);
+  }
+  bool ok = tc05::mbar_wait(&s_mbar, 0, kUWaitNs);
+  if (!ok) {
+    atomicCAS(status, 0, TL_ERR_TIMEOUT);
+    tc05::mbar_wait(&s_mbar, 0, kUWaitNs);  /* let the MMAs drain before freeing */
+  }
+  ok = __syncthreads_and(ok) != 0;  /* tcgen05.ld below is warp-collective */
+  tc05::fence_after_sync();
+  if (ok) {
+    const int sp = warp & 3, ch = warp >> 2;
+    const int row = 32 * sp + lane, gy = y0 + row;
+    float acc[32];
+    tc05::tmem_ld16(tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch, acc);
+    tc05::tmem_ld16(tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch + 16, acc + 16);
+    if (gy < H) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int gx = x0 + 32 * ch + 4 * q;
+        if (gx >= W) break;
+        const size_t i = (size_t)gy * W + gx;
+        const float4 rv = __ldg(reinterpret_cast<const float4*>(r + i));
+        const float4 sv = __ldg(reinterpret_cast<const float4*>(s + i));
+        float4 zv;
+        zv.x = sv.x * (acc[4 * q] * zscale) + sv.x * sv.x * rv.x;
+        zv.y = sv.y * (acc[4 * q + 1] * zscale) + sv.y * sv.y * rv.y;
+        zv.z = sv.z * (acc[4 * q + 2] * zscale) + sv.z * sv.z * rv.z;
+        zv.w = sv.w * (acc[4 * q + 3] * zscale) + sv.w * sv.w * rv.w;
+        *reinterpret_cast<float4*>(z + i) = zv;
+      }
+    }
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc05::fence_after_sync();
+    tc05::tmem_dealloc(tmem, kUTmemCols);
+  }
+}
+
+}  // namespace
+
+static int check_packed_shape(int H, int W) {
+  TL_REQUIRE(H >= 2 && W >= 8 && W % 4 == 0,
+             "the collapsed preconditioner needs a packed [H][W] field with W % 4 == 0");
+  TL_REQUIRE((size_t)H * W < (1ull << 31), "field too large for the collapsed preconditioner");
+  return TL_OK;
+}
+
+/* z = M^-1 r with the collapsed stencil on the tcgen05 tensor cores (umma:
+ * the Toeplitz B operands built from the network, kscale their scale). */
+int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
+                                int W, const float* r, const float* s, float* z) {
+  int rc = check_packed_shape(H, W);
+  if (rc != TL_OK) return rc;
+  const size_t n = (size_t)H * W;
+  const int nparts = std::max(1, std::min<int>(2 * ctx->num_sms, (int)((n + kThreads - 1) / kThreads)));
+  rc = tl_ensure_partials(ctx, (size_t)nparts);
+  if (rc != TL_OK) return rc;
+  rms_partial_kernel<<<nparts, kThreads, 0, ctx->stream>>>(r, n, ctx->d_part);
+  TL_CHECK_LAUNCH(ctx);
+  TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  const int tiles_x = (W + kUTW - 1) / kUTW, tiles_y = (H + kUTH - 1) / kUTH;
+  stencil_apply_tc05_kernel<<<tiles_x * tiles_y, kUThreads, 0, ctx->stream>>>(
+      H, W, tiles_x, r, s, z, reinterpret_cast<const __half*>(umma), kscale, ctx->d_part, nparts,
+      ctx->d_status);
+  TL_CHECK_LAUNCH(ctx);
+  int status = 0;
+  TL_CUDA(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (status != 0) return tl_set_error(status, "tcgen05 stencil: MMA completion wait timed out");
+  return TL_OK;
+}
+
+/* Inner flexible PCG with the collapsed learned preconditioner on packed
+ * FP32 arrays: solves A32 e = r until r.r <= tol^2 r0.r0 or max_iters steps.
+ * r is the incoming residual (the kernel leaves the final residual in r or
+ * r_alt); e, w, z, pa, pb are scratch of H*W floats, all 16-byte aligned.
+ * The step count and the final r.r land in the pinned result page. */
+int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* kscale, int H,
+                               int W, const float* kx, const float* ky, const float* s,
+                               float* r, float* r_alt, float* e, float* w, float* z, float* pa,
+                               float* pb, double tol, int max_iters, int* iters,
+                               double* rr_final) {
+  int rc = check_packed_shape(H, W);
+  if (rc != TL_OK) return rc;
+  TL_REQUIRE(max_iters >= 0 && tol > 0.0, "tl_internal_fpcg_collapsed: bad arguments");
+  const size_t n = (size_t)H * W;
+  const void* kernel = (const void*)lpcg_kernel;
+  int per_sm = 0;
+  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0));
+  TL_REQUIRE(per_sm >= 1, "the learned PCG kernel cannot be resident");
+  per_sm = std::min(per_sm, kBlocksPerSM);
+  const int G = per_sm * ctx->num_sms;
+  rc = tl_ensure_partials(ctx, (size_t)G);
+  if (rc != TL_OK) return rc;
+  TL_CUDA(cudaMemsetAsync(e, 0, n * sizeof(float), ctx->stream));
+  TL_CUDA(cudaMemsetAsync(w, 0, n * sizeof(float), ctx->stream));
+  TL_CUDA(cudaMemsetAsync(pa, 0, n * sizeof(float), ctx->stream));
+  TL_CUDA(cudaMemsetAsync(pb, 0, n * sizeof(float), ctx->stream));
+  LpcgParams P;
+  P.H = H;
+  P.W = W;
+  P.chunks = (int)((n + kChunk - 1) / kChunk);
+  P.tiles_x = (W + kTW - 1) / kTW;
+  P.tiles = P.tiles_x * ((H + kTH - 1) / kTH);
+  P.max_iters = max_iters;
+  P.tol2 = tol * tol;
+  P.kx = kx;
+  P.ky = ky;
+  P.s = s;
+  P.r0 = r;
+  P.r1 = r_alt;
+  P.e = e;
+  P.w = w;
+  P.z = z;
+  P.p0 = pa;
+  P.p1 = pb;
+  P.frag = reinterpret_cast<const uint2*>(frag);
+  P.kscale = kscale;
+  P.part = ctx->d_part;
+  P.sync = ctx->d_sync;
+  P.status = ctx->d_status;
+  P.iters_out = ctx->d_steps;
+  P.rr_out = ctx->d_result + 7;
+  TL_CUDA(cudaMemsetAsync(ctx->d_sync + TL_SYNC_BAR_COUNT, 0, 2 * sizeof(unsigned),
+                          ctx->stream));
+  TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  ctx->h_steps[0] = -1;
+  void* args[] = {&P};
+  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(kThreads), args, 0, ctx->stream));
+  TL_CHECK_LAUNCH(ctx);
+  int status = 0;
+  TL_CUDA(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (status != 0) return tl_set_error(status, "learned PCG kernel: grid-barrier timeout");
+  *iters = ((volatile int*)ctx->h_steps)[0];
+  *rr_final = ((volatile double*)ctx->h_result)[7];
+  return TL_OK;
+}

@@ -118,6 +118,20 @@ class Net:
     def adam(self, lr: float) -> None:
         check(self.lib.tl_net_adam_step(self.h, lr), "tl_net_adam_step")
 
+    def stencil(self) -> tuple[np.ndarray, float]:
+        """The 17x17 stencil K of C^T C (rows dy = -8..8, columns dx = -8..8)
+        and the FP16 scale of its tensor-core copy, both computed on the GPU."""
+        k = np.empty(17 * 17, np.float32)
+        ks = C.c_float(0.0)
+        check(self.lib.tl_net_stencil(self.h, k.ctypes.data_as(C.POINTER(C.c_float)),
+                                      C.byref(ks)), "tl_net_stencil")
+        return k.reshape(17, 17), ks.value
+
+    def apply_stencil(self, H, W, r_dev, s_dev, z_dev) -> None:
+        """z = M^-1 r on one packed [H][W] field with the collapsed stencil."""
+        check(self.lib.tl_net_apply_stencil(self.h, H, W, r_dev, s_dev, z_dev),
+              "tl_net_apply_stencil")
+
     def close(self) -> None:
         if self.h:
             self.lib.tl_net_destroy(self.h)

@@ -223,7 +223,13 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
 #define TL_METHOD_MIXED_CG 1      /* FP32 inner CG inside FP64 iterative refinement */
 #define TL_METHOD_MIXED_JACOBI 2  /* as above, Jacobi-preconditioned inner CG */
 #define TL_METHOD_MIXED_LEARNED 3 /* as above, inner flexible PCG with the learned
-                                     preconditioner (params->learned) */
+                                     preconditioner (params->learned) collapsed to
+                                     its 17x17 stencil: one persistent kernel,
+                                     tensor-core stencil; interior width % 4 == 0 */
+#define TL_METHOD_MIXED_LEARNED_LAYERS 4 /* the same solve applying the network layer
+                                     by layer (BF16 convolutions, ~25 launches per
+                                     step; H % 4 == 0, W % 64 == 0): the reference
+                                     point the collapsed stencil is checked against */
 
 typedef struct tl_solve_params {
   int method;           /* TL_METHOD_* */
@@ -281,6 +287,19 @@ int tl_net_loss_grad(tl_net* net, int H, int W, int B, int margin, const float* 
                      float* grad_host);
 /* One Adam step (beta1 0.9, beta2 0.999) with the last gradients. */
 int tl_net_adam_step(tl_net* net, float lr);
+/* The network collapsed to one stencil: C^T C is the 17x17 correlation
+ * stencil K(d) = sum_u G(u).G(u + d), G the 16-channel 9x9 kernel of the
+ * composed layers, so M^-1 r = D^-1 r + S (K * (S r)) with
+ * (K * y)(j) = sum_d K(d) y(j + d) and y zero outside the field. Rebuilt on
+ * the device whenever the weights change. host_k receives K (289 floats, row
+ * dy = -8..8, column dx = -8..8); kscale (may be NULL) the power of two that
+ * scales K before its FP16 rounding for the tensor cores. */
+int tl_net_stencil(tl_net* net, float* host_k, float* kscale);
+/* z = M^-1 r on one packed FP32 [H][W] field (W % 4 == 0) with the collapsed
+ * stencil on the tensor cores (FP16 inputs scaled by 1 / RMS(r), FP32
+ * accumulation). */
+int tl_net_apply_stencil(tl_net* net, int H, int W, const float* r, const float* s,
+                         float* z);
 /* out[b] = crop of data[meta[3b]] at rows meta[3b+1].., columns meta[3b+2]..
  * (data: device [P][HS][WS]; meta: host int triples). */
 int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, int WS,

@@ -14,6 +14,11 @@ Weight vector layout: layer 1 [tap][co] (144 floats), then layers 2..4
 [tap][ci][co] (2304 each); tap = 3*(dy+1) + (dx+1) for input offset (dy, dx).
 The gradient is derived by hand (reverse mode) and checked against central
 finite differences in tests/test_learned_oracle.py.
+
+collapse() writes the same operator as one stencil: without bias or
+activation the layers compose to a 16-channel 9x9 kernel G, and C^T C is the
+17x17 autocorrelation K of G, so that M^-1 r = s^2 r + s (K * (s r)) wherever
+the layer-by-layer zero padding plays no part (8 cells from the edge).
 """
 from __future__ import annotations
 
@@ -146,6 +151,51 @@ def loss_and_grad(w, r, s, kx, ky, margin):
     g_a1 = conv_adj(g_a2, W2)
     dW[0] += wgrad(a[0], g_a1)
     return loss, pack(dW)
+
+
+def collapse(w: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The network between its diagonal scalings as stencils: G (9 x 9 x 16),
+    C r = sum_u G(u) r(. + u), and K (17 x 17), K(d) = sum_u G(u).G(u + d),
+    the stencil of C^T C. Index [dy + R, dx + R] holds offset (dy, dx)."""
+    W1, *rest = unpack(w)
+    G = np.zeros((3, 3, CH))
+    for tap in range(9):
+        G[tap // 3, tap % 3] = W1[tap, 0]
+    for Wl in rest:
+        n = G.shape[0]
+        Gn = np.zeros((n + 2, n + 2, CH))
+        for tap in range(9):
+            dy, dx = tap // 3, tap % 3
+            # output offset u = v + t: G_new(u) += G(v) @ W[t]
+            Gn[dy:dy + n, dx:dx + n] += G @ Wl[tap]
+        G = Gn
+    K = np.zeros((17, 17))
+    for dy in range(-8, 9):
+        for dx in range(-8, 9):
+            ys = slice(max(0, -dy), min(9, 9 - dy))
+            xs = slice(max(0, -dx), min(9, 9 - dx))
+            yd = slice(max(0, dy), min(9, 9 + dy))
+            xd = slice(max(0, dx), min(9, 9 + dx))
+            K[dy + 8, dx + 8] = np.sum(G[ys, xs] * G[yd, xd])
+    return G, K
+
+
+def correlate(y: np.ndarray, K: np.ndarray) -> np.ndarray:
+    """(K * y)(j) = sum_d K(d) y(j + d) on [H, W], y zero outside."""
+    R = K.shape[0] // 2
+    H, W = y.shape
+    pad = np.zeros((H + 2 * R, W + 2 * R))
+    pad[R:R + H, R:R + W] = y
+    out = np.zeros((H, W))
+    for dy in range(-R, R + 1):
+        for dx in range(-R, R + 1):
+            out += K[dy + R, dx + R] * pad[R + dy:R + dy + H, R + dx:R + dx + W]
+    return out
+
+
+def apply_collapsed(K: np.ndarray, r: np.ndarray, s: np.ndarray) -> np.ndarray:
+    """z = s^2 r + s (K * (s r)) on one [H, W] field: the collapsed M^-1."""
+    return s * s * r + s * correlate(s * r, K)
 
 
 def loss_only(w, r, s, kx, ky, margin) -> float:

@@ -7,7 +7,10 @@ fewer inner steps than the Jacobi-preconditioned solve on unseen problems.
 Tolerances: the GPU keeps weights and activations in BF16 (8 significant
 bits) through 8 convolution layers with FP32 accumulation, against an FP64
 oracle: forward results agree to 3e-2 relative (L2), gradients to 6e-2
-relative (L2) with cosine similarity above 0.995."""
+relative (L2) with cosine similarity above 0.995. The collapsed stencil
+(tl_precond.cu) is built in FP32 on the GPU (1e-5 of the oracle's float64 K)
+and applied with FP16 inputs and FP32 sums: 1e-3 of max |z| (an FP16
+emulation of the same arithmetic in float64 gives 1.1e-4)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -162,3 +165,67 @@ def test_trained_network_beats_jacobi_on_unseen_problems(backend_built):
                     net.close()
                 g.close()
     assert steps["mixed-learned"] < steps["mixed-jacobi"] < steps["mixed"], steps
+
+
+def test_collapsed_stencil_matches_oracle(gpu):
+    """K = C^T C as a 17x17 stencil, composed on the GPU from the FP32 master
+    weights, against the float64 oracle; the FP16 scale puts max |K| in [0.5, 1)."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
+    from oracle import nn_oracle as nn
+    for w in (_weights(5), load_weights(DEFAULT_WEIGHTS)[0]):
+        net = Net(gpu, w)
+        try:
+            k, kscale = net.stencil()
+            _, want = nn.collapse(w.astype(np.float64))
+            kmax = np.abs(want).max()
+            assert np.abs(k - want).max() <= 1e-5 * kmax
+            assert 0.5 <= kscale * kmax < 1.0 + 1e-6
+        finally:
+            net.close()
+
+
+@pytest.mark.parametrize("H,W", [(72, 140), (64, 128), (130, 260)])
+def test_stencil_application_matches_oracle(gpu, H, W):
+    """z = D^-1 r + S K S r on the tensor cores against the float64 oracle, on
+    fields that fill 64 x 128 tiles exactly or leave ragged ones."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
+    from oracle import nn_oracle as nn
+    w = load_weights(DEFAULT_WEIGHTS)[0]
+    rng = np.random.default_rng(H * 1000 + W)
+    r = (1e-4 * rng.standard_normal((H, W))).astype(np.float32)
+    s = rng.uniform(0.05, 1.0, (H, W)).astype(np.float32)
+    net = Net(gpu, w)
+    try:
+        d = _upload(gpu, {"r": r, "s": s})
+        z = gpu.alloc_f32(H * W)
+        net.apply_stencil(H, W, d["r"], d["s"], z)
+        got = gpu.download_f32(z, H * W).reshape(H, W)
+        _, K = nn.collapse(w.astype(np.float64))
+        want = nn.apply_collapsed(K, r.astype(np.float64), s.astype(np.float64))
+        assert np.abs(got - want).max() <= 1e-3 * np.abs(want).max()
+    finally:
+        net.close()
+
+
+def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
+    """The same timestep solved with the fused collapsed-stencil FPCG and with
+    the network applied layer by layer: both reach the FP64 target without a
+    fall-back, with inner step counts within 5 % of each other."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
+    w, _ = load_weights(DEFAULT_WEIGHTS)
+    d = dk.random_deck(256, seed=9, end_step=1)
+    steps = {}
+    for method in ("mixed-learned", "mixed-learned-layers"):
+        g = GpuChunk(d)
+        net = Net(g.ctx, w)
+        try:
+            rep = g.solve_timestep(method, rel_tol=1e-10, learned=net)
+            assert rep["final_rel_residual"] <= 1e-10, (method, rep)
+            assert rep["fallback_events"] == 0, (method, rep)
+            steps[method] = rep["inner_steps"]
+        finally:
+            net.close()
+            g.close()
+    a, b = steps["mixed-learned"], steps["mixed-learned-layers"]
+    assert abs(a - b) <= 0.05 * b, steps

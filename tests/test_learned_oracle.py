@@ -49,3 +49,38 @@ def test_identity_weights_are_jacobi():
     assert np.allclose(z, 2 * s * s * r)
     z0 = nn.forward(np.zeros(identity_weights().size), r, s)
     assert np.allclose(z0, s * s * r)
+
+
+def test_collapsed_stencil_equals_network_away_from_the_edge():
+    """C^T C of the four linear layers is the 17x17 autocorrelation stencil K
+    of their composed 9x9 kernel: equal to the layer-by-layer network more
+    than 8 cells from the edge, for random and for the committed weights."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, load_weights
+    w_rand, r, s, _, _ = _problem(6, B=1, H=40, W=44)
+    w_trained = load_weights(DEFAULT_WEIGHTS)[0].astype(np.float64)
+    for w in (w_rand, w_trained):
+        G, K = nn.collapse(w)
+        assert G.shape == (9, 9, 16) and K.shape == (17, 17)
+        assert np.array_equal(K, K[::-1, ::-1])
+        z_net = nn.forward(w, r, s)[0]
+        z_col = nn.apply_collapsed(K, r[0], s[0])
+        scale = np.abs(z_net).max()
+        assert np.abs(z_net - z_col)[8:-8, 8:-8].max() <= 1e-12 * scale
+
+
+def test_collapsed_operator_is_symmetric_positive_definite():
+    """S K S restricted to the field is a principal submatrix of a PSD
+    Toeplitz operator, so M^-1 = D^-1 + S K S is SPD (dense check, 14 x 18)."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, load_weights
+    w = load_weights(DEFAULT_WEIGHTS)[0].astype(np.float64)
+    _, K = nn.collapse(w)
+    H, W = 14, 18
+    s = np.random.default_rng(7).uniform(0.05, 1.0, (H, W))
+    M = np.zeros((H * W, H * W))
+    for j in range(H * W):
+        e = np.zeros(H * W)
+        e[j] = 1.0
+        M[:, j] = nn.apply_collapsed(K, e.reshape(H, W), s).ravel()
+    assert np.allclose(M, M.T, rtol=0, atol=1e-12 * np.abs(M).max())
+    ev = np.linalg.eigvalsh(0.5 * (M + M.T))
+    assert ev.min() >= 0.99 * (s ** 2).min()
