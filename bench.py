@@ -271,8 +271,9 @@ def max_over_ranks(values: list[float], dist) -> list[float]:
 class Stepper:
     """One chunk and the timestep of the chosen solver."""
 
-    def __init__(self, args, solver: str, ctx):
+    def __init__(self, args, solver: str, ctx, contract: str | None = None):
         from exploringsycl_gb300.chunk import GpuChunk
+        ctx.set_fp64_contract(contract or args.fp64)
         self.solver = solver
         self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
         self.ctx = ctx
@@ -364,23 +365,35 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         h_energy.copy_(h_out)
     barrier()
 
-    # The same timesteps with plain FP64 CG under the same stop rule.
-    compare = None
+    # The same timesteps with the other solvers under the same stop rule:
+    # plain FP64 CG in both arithmetic contracts, and the mixed-precision
+    # solvers not measured above.
+    compare = []
     if args.compare and args.solver != "plain":
-        ctx2 = Context(device=local)
-        plain = Stepper(args, "cg64", ctx2)
-        cwarm = [plain.step() for _ in range(args.warmup)]
-        stream2 = torch.cuda.ExternalStream(ctx2.stream(), device=local)
-        c_ms, c_per, _, _ = timed_steps(plain, args.steps, stream2, barrier, False, local)
-        compare = {"solver": "plain FP64 CG, same stop rule",
-                   "value": c_ms / 1e3 / args.steps, "unit": UNIT,
-                   "cg_steps_per_timestep": [p["cg_steps"] for p in cwarm + c_per],
-                   "speedup": (c_ms / args.steps) / (total_ms / args.steps)}
-        if args.dump_iterations:
-            Path(args.dump_iterations).write_text(json.dumps(
-                {"size": args.size, "deck": args.deck, "stop": stop_rule("cg64"),
-                 "cg_steps": compare["cg_steps_per_timestep"]}))
-        plain.chunk.close()
+        others = [("cg64", "exact", "plain FP64 CG (exact contract, bit-identical to the "
+                                    "oracle), same stop rule"),
+                  ("cg64", "fused", "plain FP64 CG (fused multiply-add contract), "
+                                    "same stop rule")]
+        for solver in ("mixed-jacobi", "mixed-learned"):
+            if solver != args.solver:
+                others.append((solver, args.fp64, f"{solver}, same stop rule"))
+        for solver, contract, label in others:
+            ctx2 = Context(device=local)
+            other = Stepper(args, solver, ctx2, contract)
+            cwarm = [other.step() for _ in range(args.warmup)]
+            stream2 = torch.cuda.ExternalStream(ctx2.stream(), device=local)
+            c_ms, c_per, _, _ = timed_steps(other, args.steps, stream2, barrier, False, local)
+            entry = {"solver": label, "value": c_ms / 1e3 / args.steps, "unit": UNIT,
+                     "cg_steps_per_timestep": [p["cg_steps"] for p in cwarm + c_per],
+                     "speedup_of_headline": (c_ms / args.steps) / (total_ms / args.steps)}
+            compare.append(entry)
+            if args.dump_iterations and solver == "cg64" and contract == "exact":
+                Path(args.dump_iterations).write_text(json.dumps(
+                    {"size": args.size, "deck": args.deck, "stop": stop_rule("cg64"),
+                     "cg_steps": entry["cg_steps_per_timestep"]}))
+            if other.net is not None:
+                other.net.close()
+            other.chunk.close()
 
     total_ms, e2e_mean = max_over_ranks([total_ms, statistics.mean(e2e_times)], dist)
     if rank != 0:
@@ -436,7 +449,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         line["compare"] = compare
     if not args.skip_cpu:
         cpu = cpu_sample(args.size, args.cpu_iters, args.deck)
-        ref_steps = (compare["cg_steps_per_timestep"][args.warmup:] if compare
+        ref_steps = (compare[0]["cg_steps_per_timestep"][args.warmup:] if compare
                      else [p["cg_steps"] for p in per])
         mean_steps = statistics.mean(ref_steps)
         line["cpu_baseline"] = {
@@ -461,7 +474,9 @@ def main() -> None:
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--deck", choices=["random", "two-state"], default="random")
     ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned", "cg64", "plain"],
-                    default="mixed-jacobi")
+                    default="mixed-learned")
+    ap.add_argument("--fp64", choices=["exact", "fused"], default="exact",
+                    help="arithmetic contract of the persistent FP64 CG (plain, cg64, fall-back)")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
     ap.add_argument("--max-inner", type=int, default=20000,
                     help="inner steps per refinement step (smaller only for profiling captures)")

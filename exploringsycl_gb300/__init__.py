@@ -54,6 +54,7 @@ class TLSolveReport(C.Structure):
 
 METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI, METHOD_MIXED_LEARNED = 0, 1, 2, 3
 METHOD_MIXED_LEARNED_LAYERS = 4
+FP64_CONTRACTS = {"exact": 0, "fused": 1}
 METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI,
            "mixed-learned": METHOD_MIXED_LEARNED,
            "mixed-learned-layers": METHOD_MIXED_LEARNED_LAYERS}
@@ -113,6 +114,7 @@ CONTEXT_FREE = {
     "tl_copy_to_device": [_P, _P, _P, C.c_size_t],
     "tl_copy_to_host": [_P, _P, _P, C.c_size_t],
     "tl_last_solve_stats": [_P, C.POINTER(TLSolveStats)],
+    "tl_set_fp64_contract": [_P, _I],
     "tl_cg_calc_w_noalloc": [_P, _I, _I, _I, _P, _P, _P, _P, _PD],
     "tl_selftest_barrier_timeout": [_P, _I, _PI],
 }
@@ -189,6 +191,12 @@ class Context:
         self.h = C.c_void_p()
         check(self.lib.tl_context_create(device, stream, C.byref(self.h)), "tl_context_create")
         self._fields: list[int] = []
+
+    def set_fp64_contract(self, contract: str) -> None:
+        """'exact' (default) or 'fused': the arithmetic of the persistent
+        FP64 CG solve (see tl_set_fp64_contract)."""
+        check(self.lib.tl_set_fp64_contract(self.h, FP64_CONTRACTS[contract]),
+              "tl_set_fp64_contract")
 
     # -- memory
     def alloc(self, n: int) -> int:

@@ -116,6 +116,14 @@ extern "C" int tl_last_solve_stats(tl_context* ctx, tl_solve_stats* out) {
   return TL_OK;
 }
 
+extern "C" int tl_set_fp64_contract(tl_context* ctx, int contract) {
+  TL_REQUIRE(ctx, "tl_set_fp64_contract: null context");
+  TL_REQUIRE(contract == TL_FP64_EXACT || contract == TL_FP64_FUSED,
+             "tl_set_fp64_contract: unknown contract");
+  ctx->fp64_fused = contract == TL_FP64_FUSED;
+  return TL_OK;
+}
+
 extern "C" long long tl_launch_count(tl_context* ctx) {
   return ctx ? ctx->launches : -1;
 }

@@ -673,16 +673,29 @@ __device__ __forceinline__ int warp_sum8_group_of_lane(int lane) {
 
 constexpr int kWarpsPerTile = TL_GROUP / 8;  /* 8 warps x 8 groups = one tile */
 
-/* w = A p for the two cells i0, i0+1 of a lane (i0 even), contributions
- * c = w*p (0 outside the interior). kVec: the row length x is even, so the
- * pair lies in one row and every pair load is 16-byte aligned; the left and
- * right neighbours come from the adjacent lanes. Otherwise scalar loads. */
-template <bool kVec>
-__device__ __forceinline__ void w_pair(const CgPersistParams& P, unsigned i0, unsigned len,
-                                       int lane, double c[2]) {
+/* The fused contract (kFused): w = diag p with the four neighbour terms
+ * subtracted by fused multiply-adds in the order right, left, up, down. */
+__device__ __forceinline__ double smvp_fused(double dg, double a, double kr, double ar,
+                                             double kl, double al, double ku, double au,
+                                             double kd, double ad) {
+  double t = dg * a;
+  t = __fma_rn(-kr, ar, t);
+  t = __fma_rn(-kl, al, t);
+  t = __fma_rn(-ku, au, t);
+  return __fma_rn(-kd, ad, t);
+}
+
+/* w = A p for the two cells i0, i0+1 of a lane (i0 even). Returns the
+ * lane's first-level tree value of p.w: w0 p0 + w1 p1 (a cell outside the
+ * interior contributes 0), or, fused, fma(w0, p0, w1 p1). kVec: the row
+ * length x is even, so the pair lies in one row and every pair load is
+ * 16-byte aligned; the left and right neighbours come from the adjacent
+ * lanes. Otherwise scalar loads. */
+template <bool kVec, bool kFused>
+__device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, unsigned len,
+                                         int lane) {
   const int x = P.x, y = P.y, hd = P.hd;
-  c[0] = 0.0;
-  c[1] = 0.0;
+  double w0 = 0.0, w1 = 0.0, a0 = 0.0, a1 = 0.0;
   if constexpr (kVec) {
     const int jj = (int)(i0 / (unsigned)x);
     const int kk0 = (int)(i0 - (unsigned)jj * (unsigned)x);
@@ -709,18 +722,25 @@ __device__ __forceinline__ void w_pair(const CgPersistParams& P, unsigned i0, un
       kx2 = __ldg(P.kx + i0 + 2);
     }
     if (in0) {
-      const double s0 = dg.x * pc.x - (kxp.y * pc.y + kxp.x * pl) - (kyu.x * pu.x + kyp.x * pd.x);
+      const double s0 =
+          kFused ? smvp_fused(dg.x, pc.x, kxp.y, pc.y, kxp.x, pl, kyu.x, pu.x, kyp.x, pd.x)
+                 : dg.x * pc.x - (kxp.y * pc.y + kxp.x * pl) - (kyu.x * pu.x + kyp.x * pd.x);
       P.w[i0] = s0;
-      c[0] = s0 * pc.x;
+      w0 = s0;
+      a0 = pc.x;
     }
     if (in1) {
-      const double s1 = dg.y * pc.y - (kx2 * pr + kxp.y * pc.x) - (kyu.y * pu.y + kyp.y * pd.y);
+      const double s1 =
+          kFused ? smvp_fused(dg.y, pc.y, kx2, pr, kxp.y, pc.x, kyu.y, pu.y, kyp.y, pd.y)
+                 : dg.y * pc.y - (kx2 * pr + kxp.y * pc.x) - (kyu.y * pu.y + kyp.y * pd.y);
       P.w[i0 + 1] = s1;
-      c[1] = s1 * pc.y;
+      w1 = s1;
+      a1 = pc.y;
     }
   } else {
     const double* __restrict__ kx = P.kx;
     const double* __restrict__ ky = P.ky;
+    double wv[2] = {0.0, 0.0}, av[2] = {0.0, 0.0};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const unsigned i = i0 + h;
@@ -729,54 +749,69 @@ __device__ __forceinline__ void w_pair(const CgPersistParams& P, unsigned i0, un
         const int kk = (int)(i - (unsigned)jj * (unsigned)x);
         if (interior(kk, jj, x, y, hd)) {
           const double pc = __ldcg(P.p + i);
-          const double s = P.diag[i] * pc -
+          const double s =
+              kFused ? smvp_fused(P.diag[i], pc, kx[i + 1], __ldcg(P.p + i + 1), kx[i],
+                                  __ldcg(P.p + i - 1), ky[i + x], __ldcg(P.p + i + x), ky[i],
+                                  __ldcg(P.p + i - x))
+                     : P.diag[i] * pc -
                            (kx[i + 1] * __ldcg(P.p + i + 1) + kx[i] * __ldcg(P.p + i - 1)) -
                            (ky[i + x] * __ldcg(P.p + i + x) + ky[i] * __ldcg(P.p + i - x));
           P.w[i] = s;
-          c[h] = s * pc;
+          wv[h] = s;
+          av[h] = pc;
         }
       }
     }
+    w0 = wv[0]; w1 = wv[1]; a0 = av[0]; a1 = av[1];
   }
+  if (kFused) return __fma_rn(w0, a0, w1 * a1);
+  return w0 * a0 + w1 * a1;
 }
 
-/* u += alpha p, r -= alpha w for the two cells of a lane; c = r*r. */
-template <bool kVec>
-__device__ __forceinline__ void ur_pair(const CgPersistParams& P, unsigned i0, unsigned len,
-                                        double alpha, double c[2]) {
+/* u += alpha p, r -= alpha w for the two cells of a lane (fused: one
+ * rounding each); returns the lane's first-level tree value of r.r,
+ * r0 r0 + r1 r1 or, fused, fma(r0, r0, r1 r1). */
+template <bool kVec, bool kFused>
+__device__ __forceinline__ double ur_pair(const CgPersistParams& P, unsigned i0, unsigned len,
+                                          double alpha) {
   const int x = P.x, y = P.y, hd = P.hd;
-  c[0] = 0.0;
-  c[1] = 0.0;
+  auto upd_u = [alpha](double u, double p) {
+    return kFused ? __fma_rn(alpha, p, u) : u + alpha * p;
+  };
+  auto upd_r = [alpha](double r, double w) {
+    return kFused ? __fma_rn(-alpha, w, r) : r - alpha * w;
+  };
+  double r0 = 0.0, r1 = 0.0;
   if constexpr (kVec) {
     const int jj = (int)(i0 / (unsigned)x);
     const int kk0 = (int)(i0 - (unsigned)jj * (unsigned)x);
-    if (!(i0 < len && jj >= hd && jj < y - hd)) return;
-    const bool in0 = kk0 >= hd && kk0 < x - hd;
-    const bool in1 = kk0 + 1 >= hd && kk0 + 1 < x - hd;
-    if (!in0 && !in1) return;
-    const double2 uu = __ldcg(reinterpret_cast<const double2*>(P.u + i0));
-    const double2 pp = __ldcg(reinterpret_cast<const double2*>(P.p + i0));
-    const double2 rr = __ldcg(reinterpret_cast<const double2*>(P.r + i0));
-    const double2 ww = __ldcg(reinterpret_cast<const double2*>(P.w + i0));
-    if (in0 && in1) {
-      const double2 un = make_double2(uu.x + alpha * pp.x, uu.y + alpha * pp.y);
-      const double2 rn = make_double2(rr.x - alpha * ww.x, rr.y - alpha * ww.y);
-      *reinterpret_cast<double2*>(P.u + i0) = un;
-      *reinterpret_cast<double2*>(P.r + i0) = rn;
-      c[0] = rn.x * rn.x;
-      c[1] = rn.y * rn.y;
-    } else if (in0) {
-      P.u[i0] = uu.x + alpha * pp.x;
-      const double rv = rr.x - alpha * ww.x;
-      P.r[i0] = rv;
-      c[0] = rv * rv;
-    } else {
-      P.u[i0 + 1] = uu.y + alpha * pp.y;
-      const double rv = rr.y - alpha * ww.y;
-      P.r[i0 + 1] = rv;
-      c[1] = rv * rv;
+    const bool row = i0 < len && jj >= hd && jj < y - hd;
+    const bool in0 = row && kk0 >= hd && kk0 < x - hd;
+    const bool in1 = row && kk0 + 1 >= hd && kk0 + 1 < x - hd;
+    if (in0 || in1) {
+      const double2 uu = __ldcg(reinterpret_cast<const double2*>(P.u + i0));
+      const double2 pp = __ldcg(reinterpret_cast<const double2*>(P.p + i0));
+      const double2 rr = __ldcg(reinterpret_cast<const double2*>(P.r + i0));
+      const double2 ww = __ldcg(reinterpret_cast<const double2*>(P.w + i0));
+      if (in0 && in1) {
+        const double2 un = make_double2(upd_u(uu.x, pp.x), upd_u(uu.y, pp.y));
+        const double2 rn = make_double2(upd_r(rr.x, ww.x), upd_r(rr.y, ww.y));
+        *reinterpret_cast<double2*>(P.u + i0) = un;
+        *reinterpret_cast<double2*>(P.r + i0) = rn;
+        r0 = rn.x;
+        r1 = rn.y;
+      } else if (in0) {
+        P.u[i0] = upd_u(uu.x, pp.x);
+        r0 = upd_r(rr.x, ww.x);
+        P.r[i0] = r0;
+      } else {
+        P.u[i0 + 1] = upd_u(uu.y, pp.y);
+        r1 = upd_r(rr.y, ww.y);
+        P.r[i0 + 1] = r1;
+      }
     }
   } else {
+    double rv[2] = {0.0, 0.0};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const unsigned i = i0 + h;
@@ -784,14 +819,17 @@ __device__ __forceinline__ void ur_pair(const CgPersistParams& P, unsigned i0, u
         const int jj = (int)(i / (unsigned)x);
         const int kk = (int)(i - (unsigned)jj * (unsigned)x);
         if (interior(kk, jj, x, y, hd)) {
-          P.u[i] = __ldcg(P.u + i) + alpha * __ldcg(P.p + i);
-          const double rv = __ldcg(P.r + i) - alpha * __ldcg(P.w + i);
-          P.r[i] = rv;
-          c[h] = rv * rv;
+          P.u[i] = upd_u(__ldcg(P.u + i), __ldcg(P.p + i));
+          rv[h] = upd_r(__ldcg(P.r + i), __ldcg(P.w + i));
+          P.r[i] = rv[h];
         }
       }
     }
+    r0 = rv[0];
+    r1 = rv[1];
   }
+  if (kFused) return __fma_rn(r0, r0, r1 * r1);
+  return r0 * r0 + r1 * r1;
 }
 
 /* One CG step loop of TeaLeaf/drivers/cg_driver.c:18-25 with the kernels of
@@ -803,7 +841,7 @@ __device__ __forceinline__ void ur_pair(const CgPersistParams& P, unsigned i0, u
  * yields the same values as the reference's halo update; corner and outer
  * halo cells are brought up to date by the exact halo update launched after
  * the loop. */
-template <bool kVec>
+template <bool kVec, bool kFused>
 __global__ void __launch_bounds__(kPersistThreads, 1)
 cg_persistent_kernel(CgPersistParams P) {
   constexpr int kSub = kPersistThreads / 32 / kWarpsPerTile;  /* tiles per pass */
@@ -830,9 +868,7 @@ cg_persistent_kernel(CgPersistParams P) {
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
           const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
-          double c[2];
-          w_pair<kVec>(P, i0, len, lane, c);
-          v[g] = c[0] + c[1];
+          v[g] = w_pair<kVec, kFused>(P, i0, len, lane);
         }
         const double gs = warp_sum8_groups(v, lane);
         if (lane < 8) s_group[sub][wt * 8 + my_group] = gs;
@@ -857,9 +893,7 @@ cg_persistent_kernel(CgPersistParams P) {
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
           const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
-          double c[2];
-          ur_pair<kVec>(P, i0, len, alpha, c);
-          v[g] = c[0] + c[1];
+          v[g] = ur_pair<kVec, kFused>(P, i0, len, alpha);
         }
         const double gs = warp_sum8_groups(v, lane);
         if (lane < 8) s_group[sub][wt * 8 + my_group] = gs;
@@ -888,7 +922,8 @@ cg_persistent_kernel(CgPersistParams P) {
         const int jj = (int)(i / (unsigned)x);
         const int kk = (int)(i - (unsigned)jj * (unsigned)x);
         if (!interior(kk, jj, x, y, hd)) continue;
-        const double pv = beta * __ldcg(P.p + i) + __ldcg(P.r + i);
+        const double pv = kFused ? __fma_rn(beta, __ldcg(P.p + i), __ldcg(P.r + i))
+                                 : beta * __ldcg(P.p + i) + __ldcg(P.r + i);
         P.p[i] = pv;
         if (kk == hd) P.p[i - 1] = pv;
         if (kk == x - hd - 1) P.p[i + 1] = pv;
@@ -1205,8 +1240,11 @@ int tl_internal_cg64_loop(tl_context* ctx, int x, int y, int hd, double eps, int
 
   int per_sm = 0;
   /* Pair loads need an even row length (16-byte aligned pairs in one row). */
-  const void* kernel = (x % 2 == 0) ? (const void*)cg_persistent_kernel<true>
-                                    : (const void*)cg_persistent_kernel<false>;
+  const void* kernel =
+      ctx->fp64_fused ? ((x % 2 == 0) ? (const void*)cg_persistent_kernel<true, true>
+                                      : (const void*)cg_persistent_kernel<false, true>)
+                      : ((x % 2 == 0) ? (const void*)cg_persistent_kernel<true, false>
+                                      : (const void*)cg_persistent_kernel<false, false>);
   TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, 0));
   TL_REQUIRE(per_sm >= 1, "persistent CG kernel cannot be resident");
   const int tiles_per_block = kPersistThreads / 32 / kWarpsPerTile;

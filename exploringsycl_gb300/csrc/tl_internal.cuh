@@ -80,6 +80,7 @@ struct tl_context {
   cudaEvent_t ev_start = nullptr;  /* around the persistent kernel of a solve */
   cudaEvent_t ev_stop = nullptr;
   tl_solve_stats last_solve = {0.0f, 0, 0};
+  int fp64_fused = 0;             /* TL_FP64_FUSED: the persistent FP64 CG uses FMAs */
 };
 
 /* Thread-local error message and helpers (tl_context.cu). */

@@ -90,6 +90,21 @@ const char* tl_last_error(void);
 /* Number of this library's kernel launches issued on the context so far. */
 long long tl_launch_count(tl_context* ctx);
 
+/* Arithmetic contract of the persistent FP64 CG solve (tl_cg_solve, the
+ * run-ahead path of run_cg_init, and TL_METHOD_CG64). TL_FP64_EXACT (the
+ * default): no fused multiply-adds, each operation rounded as the
+ * reference's C kernels compiled without contraction, bit-identical to the
+ * CPU oracle. TL_FP64_FUSED: the stencil as diag*p followed by four fused
+ * multiply-adds (right, left, up, down neighbours), u += alpha p,
+ * r -= alpha w and p = beta p + r as single fused operations, and the first
+ * level of each dot-product tree as fma(a0, b0, a1*b1): 11 instead of 19
+ * FP64 instructions per cell and step, bit-identical to the oracle's fused
+ * mode. No counterpart in the reference (whose GPU builds leave contraction
+ * to the compiler). The step-wise kernels always use the exact contract. */
+#define TL_FP64_EXACT 0
+#define TL_FP64_FUSED 1
+int tl_set_fp64_contract(tl_context* ctx, int contract);
+
 /* -------------------------------------------------------------- fields
  * Replace the SYCL buffers of kernel_initialise / kernel_finalise
  * (TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:31-125). */

@@ -48,6 +48,9 @@ SIGNATURES = {
     "orc_cg_calc_w": ([_I, _I, _I, _A, _A, _A, _A, _PD], None),
     "orc_cg_calc_ur": ([_I, _I, _I, _A, _A, _A, _A, _D, _PD], None),
     "orc_cg_calc_p": ([_I, _I, _I, _D, _A, _A], None),
+    "orc_cg_calc_w_fused": ([_I, _I, _I, _A, _A, _A, _A, _PD], None),
+    "orc_cg_calc_ur_fused": ([_I, _I, _I, _A, _A, _A, _A, _D, _PD], None),
+    "orc_cg_calc_p_fused": ([_I, _I, _I, _D, _A, _A], None),
     "orc_copy_u": ([_I, _I, _I, _A, _A], None),
     "orc_calculate_residual": ([_I, _I, _I, _A, _A, _A, _A, _A], None),
     "orc_calculate_2norm": ([_I, _I, _I, _A, _PD], None),
@@ -163,11 +166,17 @@ class OracleChunk:
         dt = self.deck.initial_timestep
         return dt / (self.dx * self.dx), dt / (self.dy * self.dy)
 
-    def cg_timestep(self, max_iters=None, rel_tol=None):
+    def cg_timestep(self, max_iters=None, rel_tol=None, contract="exact"):
         """One timestep of the reference CG driver; returns the number of
         main steps executed and records pw/rrn of each. With rel_tol the stop
-        rule becomes sqrt(rr) < rel_tol * ||u0||_2 instead of eps."""
+        rule becomes sqrt(rr) < rel_tol * ||u0||_2 instead of eps. contract
+        'fused' uses the fused multiply-add kernels of the GPU's
+        TL_FP64_FUSED persistent solve."""
         L, x, y, hd = self.L, self.x, self.y, self.hd
+        fused = contract == "fused"
+        calc_w = L.orc_cg_calc_w_fused if fused else L.orc_cg_calc_w
+        calc_ur = L.orc_cg_calc_ur_fused if fused else L.orc_cg_calc_ur
+        calc_p = L.orc_cg_calc_p_fused if fused else L.orc_cg_calc_p
         max_iters = self.deck.max_iters if max_iters is None else max_iters
         rx, ry = self.rx_ry()
         self.halos(["energy", "density"], 2)
@@ -190,14 +199,13 @@ class OracleChunk:
         steps = 0
         for tt in range(max_iters):
             pw = C.c_double(0.0)
-            L.orc_cg_calc_w(x, y, hd, self.p("w"), self.p("p"), self.p("kx"), self.p("ky"),
-                            _pd(pw))
+            calc_w(x, y, hd, self.p("w"), self.p("p"), self.p("kx"), self.p("ky"), _pd(pw))
             alpha = rro_v / pw.value
             rrn = C.c_double(0.0)
-            L.orc_cg_calc_ur(x, y, hd, self.p("u"), self.p("r"), self.p("p"), self.p("w"),
-                             alpha, _pd(rrn))
+            calc_ur(x, y, hd, self.p("u"), self.p("r"), self.p("p"), self.p("w"), alpha,
+                    _pd(rrn))
             beta = rrn.value / rro_v
-            L.orc_cg_calc_p(x, y, hd, beta, self.p("p"), self.p("r"))
+            calc_p(x, y, hd, beta, self.p("p"), self.p("r"))
             self.pw_hist.append(pw.value)
             self.rrn_hist.append(rrn.value)
             rro_v = rrn.value

@@ -390,6 +390,91 @@ void orc_cg_calc_p(int x, int y, int halo_depth, double beta, double* p,
   }
 }
 
+/* ------------------------------------------------ fused FP64 contract
+ * The arithmetic of the GPU's TL_FP64_FUSED persistent CG
+ * (include/tealeaf_gb300.h, tl_set_fp64_contract): C's fma() is correctly
+ * rounded, as the GPU's fused multiply-add. The reduction order is the
+ * reference's; only the first tree level pairs (a0*b0, a1*b1) become
+ * fma(a0, b0, a1*b1). */
+
+static double orc_tree64_fused(const double* ca, const double* cb) {
+  double a[WG];
+  for (int i = 0; i < WG; i += 2) a[i] = fma(ca[i], cb[i], ca[i + 1] * cb[i + 1]);
+  for (int stride = 2; stride < WG; stride *= 2) {
+    for (int i = 0; i < WG; i += 2 * stride) a[i] = a[i] + a[i + stride];
+  }
+  return a[0];
+}
+
+/* As REDUCING_KERNEL; BODY assigns the factors ca, cb of the cell's term
+ * (0, 0 outside the interior). */
+#define REDUCING_KERNEL_FUSED(result, BODY)                             \
+  do {                                                                  \
+    long len_ = (long)x * (long)y;                                      \
+    long ng_ = (len_ + WG - 1) / WG;                                    \
+    double* part_ = (double*)malloc(sizeof(double) * (size_t)ng_);      \
+    _Pragma("omp parallel for schedule(static)")                        \
+    for (long g_ = 0; g_ < ng_; ++g_) {                                 \
+      double a_[WG], b_[WG];                                            \
+      for (int l_ = 0; l_ < WG; ++l_) {                                 \
+        long i = g_ * WG + l_;                                          \
+        double ca = 0.0, cb = 0.0;                                      \
+        if (i < len_) {                                                 \
+          const int kk = (int)(i % x);                                  \
+          const int jj = (int)(i / x);                                  \
+          if (INTERIOR(kk, jj)) { BODY }                                \
+        }                                                               \
+        a_[l_] = ca;                                                    \
+        b_[l_] = cb;                                                    \
+      }                                                                 \
+      part_[g_] = orc_tree64_fused(a_, b_);                             \
+    }                                                                   \
+    result = reduce_levels(part_, ng_);                                 \
+    free(part_);                                                        \
+  } while (0)
+
+/* w = A p as diag*p minus the right, left, up and down neighbour terms by
+ * fused multiply-adds, diag grouped as in smvp(); pw accumulated. */
+void orc_cg_calc_w_fused(int x, int y, int halo_depth, double* w, const double* p,
+    const double* kx, const double* ky, double* pw) {
+  double s;
+  REDUCING_KERNEL_FUSED(s, {
+    const double diag = 1.0 + (kx[i + 1] + kx[i]) + (ky[i + x] + ky[i]);
+    double t = diag * p[i];
+    t = fma(-kx[i + 1], p[i + 1], t);
+    t = fma(-kx[i], p[i - 1], t);
+    t = fma(-ky[i + x], p[i + x], t);
+    t = fma(-ky[i], p[i - x], t);
+    w[i] = t;
+    ca = t;
+    cb = p[i];
+  });
+  *pw += s;
+}
+
+void orc_cg_calc_ur_fused(int x, int y, int halo_depth, double* u, double* r,
+    const double* p, const double* w, double alpha, double* rrn) {
+  double s;
+  REDUCING_KERNEL_FUSED(s, {
+    u[i] = fma(alpha, p[i], u[i]);
+    r[i] = fma(-alpha, w[i], r[i]);
+    ca = r[i];
+    cb = r[i];
+  });
+  *rrn = s;
+}
+
+void orc_cg_calc_p_fused(int x, int y, int halo_depth, double beta, double* p,
+    const double* r) {
+  long len = (long)x * y;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < len; ++i) {
+    const int kk = (int)(i % x);
+    const int jj = (int)(i / x);
+    if (INTERIOR(kk, jj)) p[i] = fma(beta, p[i], r[i]);
+  }
+}
+
 /* -------------------------------------------------------- solver methods */
 
 /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:7-31 */

@@ -107,6 +107,13 @@ void orc_cg_calc_ur(int x, int y, int halo_depth, double* u, double* r,
     const double* p, const double* w, double alpha, double* rrn);
 void orc_cg_calc_p(int x, int y, int halo_depth, double beta, double* p,
     const double* r);
+/* The fused FP64 contract of the GPU's persistent CG (TL_FP64_FUSED). */
+void orc_cg_calc_w_fused(int x, int y, int halo_depth, double* w, const double* p,
+    const double* kx, const double* ky, double* pw);
+void orc_cg_calc_ur_fused(int x, int y, int halo_depth, double* u, double* r,
+    const double* p, const double* w, double alpha, double* rrn);
+void orc_cg_calc_p_fused(int x, int y, int halo_depth, double beta, double* p,
+    const double* r);
 
 /* --- shared solver methods (TeaLeaf/c_kernels/sycl/solver_methods.cpp) --- */
 void orc_copy_u(int x, int y, int halo_depth, const double* u, double* u0);

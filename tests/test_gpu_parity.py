@@ -67,6 +67,32 @@ def test_fused_cg_timesteps_bitwise(name, backend_built, oracle_built):
         g.close()
 
 
+@pytest.mark.parametrize("name", list(DECKS))
+def test_fused_contract_cg_timesteps_bitwise(name, backend_built, oracle_built):
+    """The TL_FP64_FUSED persistent solve against the oracle's fused-multiply-
+    add kernels: step counts, per-step scalars, fields and summary bit for
+    bit; and against the exact contract, the field summary within 1e-10."""
+    g, c = _pair(name, backend_built, oracle_built)
+    g.ctx.set_fp64_contract("fused")
+    exact = oracle_built.OracleChunk(DECKS[name]())
+    try:
+        for step in range(2):
+            gs = g.cg_timestep()
+            cs = c.cg_timestep(contract="fused")
+            exact.cg_timestep()
+            assert gs == cs, (step, gs, cs)
+            assert g.rro0 == c.rro0
+            assert _same(g.pw_hist[:gs], np.array(c.pw_hist))
+            assert _same(g.rrn_hist[:gs], np.array(c.rrn_hist))
+            for f in ("u", "u0", "p", "r", "w", "energy"):
+                assert _same(g.read(f), c.f[f]), (step, f)
+            assert g.summary() == c.summary()
+            for a_, b_ in zip(g.summary(), exact.summary()):
+                assert abs(a_ - b_) <= 1e-10 * abs(b_)
+    finally:
+        g.close()
+
+
 def _stepwise_gpu_timestep(g, max_iters):
     """The CG driver loop over the step-wise entry points."""
     x, y, hd, f = g.x, g.y, g.hd, g.f

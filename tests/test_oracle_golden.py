@@ -125,3 +125,17 @@ def test_deck_round_trip_through_driver(tmp_path, oracle_built):
     log = (tmp_path / "tea.out").read_text()
     assert f"grid_x_cells = 24" in log
     assert log.count("state ") == len(d.states)
+
+
+def test_fused_contract_agrees_with_exact_to_1e10(oracle_built):
+    """The oracle's fused multiply-add CG (the GPU's TL_FP64_FUSED contract)
+    against the exact contract on the reference's two-state and five-state
+    decks: field summaries within 1e-10 relative, step counts within one."""
+    from exploringsycl_gb300 import deck as dk
+    for d in (dk.five_state(64, end_step=2), dk.two_state(96, end_step=2)):
+        a, b = oracle_built.OracleChunk(d), oracle_built.OracleChunk(d)
+        for _ in range(2):
+            sa, sb = a.cg_timestep(), b.cg_timestep(contract="fused")
+            assert abs(sa - sb) <= 1
+            for x, y in zip(a.summary(), b.summary()):
+                assert abs(x - y) <= 1e-10 * abs(x)
