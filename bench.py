@@ -5,13 +5,17 @@ Default workload (the headline): the seeded random-state deck at 4096 x 4096
 cells (20-60 rectangles and discs, density log-uniform in [0.05, 200], energy
 uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
 1/density; each timestep solved until the FP64 true residual satisfies
-||u0 - A u||_2 <= 1e-10 ||u0||_2, with the mixed-precision Jacobi-PCG solver
-(FP32 inner solve, FP64 refinement). The same timesteps are also solved with
-plain FP64 CG under the same stop rule (the `compare` object). A step is one
+||u0 - A u||_2 <= 1e-10 ||u0||_2, with the learned + mixed-precision solver:
+FP32 inner flexible PCG whose preconditioner is the trained network collapsed
+to one 17x17 stencil (tensor cores), inside FP64 iterative refinement. The
+same timesteps are also solved, under the same stop rule, with plain FP64 CG
+in both arithmetic contracts (exact / fused multiply-add) and with the
+mixed-precision Jacobi-PCG solver (the `compare` list). A step is one
 timestep (TeaLeaf/diffuse.c:23-78): halo update, the solve, residual / norm /
 finalise. Timesteps follow one another (warm-up steps are timesteps 1..W).
 `--solver plain --deck two-state` is the drop-in configuration: the
-reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000.
+reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000
+(`--fp64 fused` for the fused multiply-add contract).
 
 Reported:
   value      device time per timestep (CUDA events on the library's stream,
@@ -19,9 +23,10 @@ Reported:
   e2e        the same timestep through the C ABI with host buffers: density
              and energy copied in from pinned host memory, energy and the
              field summary copied back, inside the timed region
-  roofline   the dominant kernel (the persistent inner FP32 CG kernel, or the
-             FP64 CG kernel for plain/cg64): algorithmic bytes / kernel time
-             against the measured HBM copy bandwidth
+  roofline   the dominant kernel (the persistent inner FP32 kernel of the
+             mixed solver, or the FP64 CG kernel for plain/cg64): algorithmic
+             bytes / kernel time against the measured HBM copy bandwidth; for
+             the FP64 kernel also FP64 instructions / s against the FP64 peak
   cpu_baseline  the CPU oracle (restatement of the reference's kernels) on
              this host's cores: plain FP64 CG steps of timestep 1 timed and
              scaled by the CG step count of each timestep under the same stop
@@ -57,15 +62,20 @@ BYTES_PER_CELL_STEP = 104          # calc_w 32 + calc_ur 48 + calc_p 24 (FP64)
 # reads in both phases (8 B).
 INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
 # Learned FPCG step (collapsed stencil, one persistent kernel): phase P reads
-# z, p_old, kx, ky and writes p_new, w (24 B); phase Z reads r, w, s, p_new, e
-# and writes r, e, z (32 B).
-LEARNED_BYTES = 56
-FP64_OPS_PER_CELL_STEP = 19        # FP64 instructions per cell of the exact CG step
+# z, p_old, kx, ky, e and writes p_new, w, e (32 B); phase Z reads r, w, s and
+# writes r, z (20 B).
+LEARNED_BYTES = 52
+# FP64 instructions per cell of one CG step: exact contract (stencil 9 with the
+# precomputed diagonal, dot products 2 x 1.6, u/r update 4, p update 2) and fused
+# multiply-add contract (stencil 5, dot products 2 x 1.6, u/r 2, p 1).
+FP64_OPS_PER_CELL_STEP = {"exact": 19, "fused": 11}
 # dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
 # each persistent kernel, from one ncu capture (profiles/*.txt).
 NCU_BYTES_PER_CELL_STEP = {
-    "cg_persistent_kernel": 112.3,  # profiles/cg_persistent_fp64_4096.txt (104 + diag 8)
-    "inner_cg_kernel": 51.3,        # profiles/inner_cg_mixed_jacobi_4096.txt
+    ("cg_persistent_kernel", "exact"): 115.4,  # profiles/cg_persistent_fp64_exact_4096.txt
+    ("cg_persistent_kernel", "fused"): 120.1,  # profiles/cg_persistent_fp64_fused_4096.txt
+    ("inner_cg_kernel", None): 51.3,           # profiles/inner_cg_mixed_jacobi_4096.txt
+    ("lpcg_kernel", None): 50.6,               # profiles/lpcg_learned_4096.txt
 }
 ITER_FIXTURES = {"two-state": ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json",
                  "random": ROOT / "tests" / "golden" / "cg_iterations_random_4096.json"}
@@ -412,16 +422,18 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
     achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9
     traffic = None
-    if NCU_BYTES_PER_CELL_STEP.get(kernel) is not None:
-        traffic = NCU_BYTES_PER_CELL_STEP[kernel] * cells * k_steps
+    key = (kernel, args.fp64 if kernel == "cg_persistent_kernel" else None)
+    if NCU_BYTES_PER_CELL_STEP.get(key) is not None:
+        # ncu DRAM bytes per cell and step x the cells and steps of one timestep
+        traffic = NCU_BYTES_PER_CELL_STEP[key] * cells * k_steps
     roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
             "peak_source": peaks["source"], "traffic": traffic, "bytes_per_cell_step": bpc,
             "kernel_ms_per_step_avg": k_ms, "kernel_steps_per_timestep": k_steps}
     if kernel == "cg_persistent_kernel":
-        gops = FP64_OPS_PER_CELL_STEP * cells * k_steps / (k_ms * 1e-3) / 1e9
-        roof.update({"fp64_gops": gops, "fp64_peak_gops": FP64_PEAK_GOPS,
-                     "fp64_frac": gops / FP64_PEAK_GOPS})
+        gops = FP64_OPS_PER_CELL_STEP[args.fp64] * cells * k_steps / (k_ms * 1e-3) / 1e9
+        roof.update({"fp64_contract": args.fp64, "fp64_gops": gops,
+                     "fp64_peak_gops": FP64_PEAK_GOPS, "fp64_frac": gops / FP64_PEAK_GOPS})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
