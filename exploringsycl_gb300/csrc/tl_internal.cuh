@@ -111,7 +111,7 @@ int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
                             const float** kscale);
 int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
                                 int W, const float* r, const float* s, float* z);
-int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* kscale, int H,
+int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
                                int W, const float* kx, const float* ky, const float* s,
                                float* r, float* r_alt, float* e, float* w, float* z, float* pa,
                                float* pb, double tol, int max_iters, int* iters,

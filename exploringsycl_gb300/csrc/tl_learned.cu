@@ -474,6 +474,7 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
 constexpr int kStencil = 17;            /* C^T C: 17 x 17 taps */
 constexpr int kFragEntries = 17 * 2 * 2 * 32;
 constexpr int kUmmaHalves = 17 * 2 * 256;  /* 34 B operands of 16 x 16 FP16 */
+constexpr int kUmma32Halves = 17 * 512;    /* 17 B operands of 32 x 16 FP16 */
 
 /* Composes the four layers into the 16-channel 9x9 kernel G of C (G(u)
  * multiplies the input at offset u), then K(d) = sum_u G(u).G(u + d), the
@@ -483,12 +484,16 @@ constexpr int kUmmaHalves = 17 * 2 * 256;  /* 34 B operands of 16 x 16 FP16 */
  * n = g (lane = 4 g + t), as FP16 pairs, K scaled by kscale = 2^-ceil(log2 max|K|).
  * umma holds the same Toeplitz blocks as tcgen05 B operands: matrix
  * (dy, kb) at halves 256 (2 dy + kb), element (n, k) = T(k, n) at
- * (k / 8) 128 + 8 n + k % 8 (K-major core matrices, 16 x 16).
+ * (k / 8) 128 + 8 n + k % 8 (K-major core matrices, 16 x 16). umma32 holds,
+ * per dy, the 32 x 16 operand of one 16-column input window and the 32
+ * output columns it reaches: element (n, k) = K(dy, k + 8 - n) at halves
+ * 512 dy + (k / 8) 256 + 8 n + k % 8.
  * One block; runs whenever the weights change. */
 __global__ void __launch_bounds__(256) collapse_kernel(const float* __restrict__ master,
                                                         float* __restrict__ k_out,
                                                         uint2* __restrict__ frag,
                                                         __half* __restrict__ umma,
+                                                        __half* __restrict__ umma32,
                                                         float* __restrict__ kscale_out) {
   __shared__ float s_g[2][81 * kCh];
   __shared__ float s_k[kStencil * kStencil];
@@ -568,6 +573,11 @@ __global__ void __launch_bounds__(256) collapse_kernel(const float* __restrict__
     const int k = (e >> 7) * 8 + (e & 7), n = (e >> 3) & 15;
     umma[i] = __float2half_rn(tap(dyi - 8, 16 * kb + k - 8 - n));
   }
+  for (int i = tid; i < kUmma32Halves; i += blockDim.x) {
+    const int dyi = i >> 9, e = i & 511;
+    const int k = (e >> 8) * 8 + (e & 7), n = (e >> 3) & 31;
+    umma32[i] = __float2half_rn(tap(dyi - 8, k + 8 - n));
+  }
 }
 
 }  // namespace
@@ -606,6 +616,7 @@ struct tl_net {
   float* stencil_k = nullptr;     /* K, 289 floats */
   uint2* stencil_frag = nullptr;  /* tensor-core fragments of K * kscale (FP16) */
   __half* stencil_umma = nullptr; /* the same as tcgen05 B operands */
+  __half* stencil_umma32 = nullptr; /* window operands of N = 32 (persistent solve) */
   float* stencil_kscale = nullptr;
 };
 
@@ -744,7 +755,7 @@ static int refresh_weights(tl_net* net) {
   TL_CHECK_LAUNCH(net->ctx);
   collapse_kernel<<<1, 256, 0, net->ctx->stream>>>(net->master, net->stencil_k,
                                                     net->stencil_frag, net->stencil_umma,
-                                                    net->stencil_kscale);
+                                                    net->stencil_umma32, net->stencil_kscale);
   TL_CHECK_LAUNCH(net->ctx);
   return TL_OK;
 }
@@ -1025,6 +1036,7 @@ extern "C" int tl_net_create(tl_context* ctx, tl_net** out) {
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_k, kStencil * kStencil * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_frag, kFragEntries * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_umma, kUmmaHalves * sizeof(__half));
+  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_umma32, kUmma32Halves * sizeof(__half));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_kscale, sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(net->master, 0, np * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(net->adam_m, 0, np * sizeof(float));
@@ -1045,6 +1057,7 @@ extern "C" int tl_net_destroy(tl_net* net) {
   cudaFree(net->dadj); cudaFree(net->partial);
   cudaFree(net->stencil_k); cudaFree(net->stencil_frag); cudaFree(net->stencil_kscale);
   cudaFree(net->stencil_umma);
+  cudaFree(net->stencil_umma32);
   for (auto& a : net->act) cudaFree(a);
   for (auto& a : net->bct) cudaFree(a);
   cudaFree(net->b0); cudaFree(net->q); cudaFree(net->gz); cudaFree(net->g16a);
@@ -1133,7 +1146,7 @@ int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
                             const float** kscale) {
   TL_REQUIRE(net && frag && umma && kscale, "tl_internal_net_stencil: null argument");
   *frag = net->stencil_frag;
-  *umma = net->stencil_umma;
+  *umma = net->stencil_umma32;
   *kscale = net->stencil_kscale;
   return TL_OK;
 }

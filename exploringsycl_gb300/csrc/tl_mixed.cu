@@ -522,7 +522,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
           const float* kscale = nullptr;
           rc = tl_internal_net_stencil(prm->learned, &frag, &umma, &kscale);
           if (rc != TL_OK) return rc;
-          rc = tl_internal_fpcg_collapsed(ctx, frag, kscale, H, W, kx32, ky32, invd, r32, r32b,
+          rc = tl_internal_fpcg_collapsed(ctx, umma, kscale, H, W, kx32, ky32, invd, r32, r32b,
                                           e32, w32, z32, pa, pb, tol, prm->max_inner, &it,
                                           &rr_in);
         }

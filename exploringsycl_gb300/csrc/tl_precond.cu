@@ -64,21 +64,41 @@
 
 namespace {
 
-constexpr int kTH = 64;                 /* phase Z tile rows */
-constexpr int kTW = 64;                 /* phase Z tile columns */
-constexpr int kWarpsX = kTW / 32;       /* a warp owns 16 rows x 32 columns */
-constexpr int kThreads = 32 * kWarpsX * (kTH / 16);
-constexpr int kBlocksPerSM = 4;
+constexpr int kThreads = 1024;          /* 32 warps, one block per SM */
+constexpr int kWorkers = kThreads - 32; /* phase Z: warps 1..31; warp 0 issues the MMAs */
 constexpr int kChunk = 4 * kThreads;    /* phase P: cells per block iteration */
 constexpr int kHalo = 8;
-constexpr int kRows = kTH + 2 * kHalo;  /* staged rows */
-constexpr int kCols = kTW + 2 * kHalo;  /* staged columns */
-/* halves per staged row: a multiple of 8 (16-byte ldmatrix rows) whose word
- * stride is 4 x odd modulo 32, so the 8 rows of an ldmatrix phase fall in
- * distinct banks */
-constexpr int kStride = kCols + 8;
-static_assert(kStride % 8 == 0 && ((kStride / 2) % 8) == 4, "bank-conflicting row stride");
-constexpr int kFrag = 17 * 2 * 2 * 32;  /* uint2 entries of the Toeplitz fragment table */
+constexpr int kTH = 128;                /* tile rows = MMA M = tensor-memory lanes */
+constexpr int kTW = 64;                 /* tile columns */
+constexpr int kRows = kTH + 2 * kHalo;  /* 144 staged rows */
+constexpr int kGroups = (kTW + 2 * kHalo) / 4;  /* float4 groups per staged row */
+constexpr int kWindows = kTW / 16 + 1;          /* 16-column input windows per tile */
+/* A operand: ten K-major chunks of 8 staged columns, each 144 rows x 16 B,
+ * +16 B so that the 8-byte stores of one staged row spread over the banks */
+constexpr int kChunkBytes = kRows * 16 + 16;
+constexpr int kABytes = (kTW + 2 * kHalo) / 8 * kChunkBytes;
+constexpr int kABuf = (kABytes + 127) / 128 * 128;
+constexpr int kBBytes = 17 * 1024;      /* 17 B operands (one per dy) of 32 x 16 FP16 */
+constexpr int kZStride = kTW + 4;       /* floats per row of the accumulator hand-over */
+/* accumulators per buffer: even windows into columns 0..95 (tile column c at
+ * 16 + c), odd windows into 96..159 (tile column c at 96 + c); two buffers */
+constexpr uint32_t kDCols = 160;
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kIdesc = tc05::idesc_f16_f32<kTH, 32>();
+constexpr unsigned long long kWaitNs = 1000000000ull;  /* bound of every mbarrier wait */
+constexpr int kReaders = 8;             /* warps 4..11 move accumulators to shared memory */
+constexpr int kBarWorkers = 1;          /* named barrier of the worker warps */
+
+/* dynamic shared memory */
+constexpr int kOffA0 = 0;
+constexpr int kOffA1 = kABuf;
+constexpr int kOffB = 2 * kABuf;
+constexpr int kOffZ = kOffB + kBBytes;
+constexpr int kOffBar = kOffZ + kTH * kZStride * 4;  /* a_full[2] mma_done[2] d_free[2] drain */
+constexpr int kOffTmem = kOffBar + 7 * 8;
+constexpr int kLpcgSmem = (kOffTmem + 8 + 127) / 128 * 128;
+static_assert(kOffB % 128 == 0 && kOffZ % 16 == 0 && kOffBar % 8 == 0, "alignment");
+static_assert(2 * kDCols <= kTmemCols, "tensor memory");
 
 struct LpcgParams {
   int H, W, chunks, tiles_x, tiles, max_iters;
@@ -86,7 +106,7 @@ struct LpcgParams {
   const float *kx, *ky, *s;
   float *r0, *r1;  /* residual, double-buffered (r0 holds the incoming one) */
   float *e, *w, *z, *p0, *p1;
-  const uint2* frag;
+  const __half* umma;  /* window B operands, 17 x 32 x 16 FP16 */
   const float* kscale;
   double* part;  /* 4 arrays of gridDim.x partial sums */
   unsigned* sync;
@@ -107,7 +127,7 @@ __device__ __forceinline__ float block_sum(float v, float* s_red) {
   v = warp_sum(v);
   if (lane == 0) s_red[warp] = v;
   __syncthreads();
-  float t = lane < (kThreads / 32) ? s_red[lane] : 0.0f;
+  float t = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0.0f;
   t = warp_sum(t);
   __syncthreads();
   return t;
@@ -130,103 +150,17 @@ __device__ __forceinline__ double sum_partials(const double* part, int n, double
   return t;
 }
 
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint2 b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
-      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
-}
-
-__device__ __forceinline__ void ldmatrix_x4(uint32_t a[4], const __half* src) {
-  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(src);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
-               : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
-               : "r"(addr));
-}
-
 __device__ __forceinline__ float4 ld4(const float* p) {
   return __ldcg(reinterpret_cast<const float4*>(p));
 }
-__device__ __forceinline__ float2 ld2(const float* p) {
-  return __ldcg(reinterpret_cast<const float2*>(p));
+
+__device__ __forceinline__ void named_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;\n" :: "r"(id), "r"(n) : "memory");
 }
 
-/* Stages y = sigma * s * (r - alpha w) for tile rows y0-8 .. y0+71 and columns
- * x0-8 .. x0+135 as FP16 (zero outside the domain). W % 4 == 0, so a group of
- * four columns is entirely inside or outside. w may be null (alpha = 0). Each
- * thread issues the loads of two groups before it converts and stores them. */
-__device__ __forceinline__ void stage_tile(int H, int W, int y0, int x0, const float* rold,
-                                           const float* w, const float* s, float alpha,
-                                           float sigma, __half* s_y) {
-  constexpr int kGroups = kCols / 4;
-  constexpr int kTotal = kRows * kGroups;
-  for (int q0 = threadIdx.x; q0 < kTotal; q0 += 2 * kThreads) {
-    float4 r[2], ww[2], ss[2];
-    bool in[2];
-    int off[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int q = q0 + u * kThreads;
-      const int row = q / kGroups, grp = q - row * kGroups;
-      const int gy = y0 - kHalo + row, gx = x0 - kHalo + 4 * grp;
-      off[u] = row * kStride + 4 * grp;
-      in[u] = q < kTotal && gy >= 0 && gy < H && gx >= 0 && gx < W;
-      r[u] = ww[u] = ss[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (in[u]) {
-        const size_t i = (size_t)gy * W + gx;
-        r[u] = ld4(rold + i);
-        if (w) ww[u] = ld4(w + i);
-        ss[u] = __ldg(reinterpret_cast<const float4*>(s + i));
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (q0 + u * kThreads >= kTotal) break;
-      const float4 rv = make_float4(r[u].x - alpha * ww[u].x, r[u].y - alpha * ww[u].y,
-                                    r[u].z - alpha * ww[u].z, r[u].w - alpha * ww[u].w);
-      const __half2 lo = __floats2half2_rn(sigma * ss[u].x * rv.x, sigma * ss[u].y * rv.y);
-      const __half2 hi = __floats2half2_rn(sigma * ss[u].z * rv.z, sigma * ss[u].w * rv.w);
-      uint2 packed;
-      packed.x = *reinterpret_cast<const uint32_t*>(&lo);
-      packed.y = *reinterpret_cast<const uint32_t*>(&hi);
-      *reinterpret_cast<uint2*>(s_y + off[u]) = packed;
-    }
-  }
-}
-
-/* acc[j] = (K * y) for this warp's 16 x 32 block: rows wr.., columns
- * wc + 8j.., in the m16n8 accumulator layout. */
-__device__ __forceinline__ void stencil_mma(const __half* s_y, const uint2* s_frag, int wr,
-                                            int wc, float acc[4][4]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int j = 0; j < 4; ++j)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[j][q] = 0.0f;
-  const __half* base = s_y + (wr + (lane & 15)) * kStride + wc + (lane >> 4) * 8;
-#pragma unroll 1
-  for (int dyi = 0; dyi < 17; ++dyi) {
-    uint32_t a0[4], a1[4];
-    const __half* src = base + dyi * kStride;
-    const uint2* f = s_frag + dyi * 128 + lane;
-    const uint2 b00 = f[0], b01 = f[32], b10 = f[64], b11 = f[96];
-    ldmatrix_x4(a0, src);
-    ldmatrix_x4(a1, src + 16);
-    mma16816(acc[0], a0, b00);
-    mma16816(acc[0], a1, b01);
-    mma16816(acc[1], a0, b10);
-    mma16816(acc[1], a1, b11);
-    ldmatrix_x4(a0, src + 32);
-    mma16816(acc[2], a1, b00);
-    mma16816(acc[2], a0, b01);
-    mma16816(acc[3], a1, b10);
-    mma16816(acc[3], a0, b11);
-  }
-}
-
-__device__ __forceinline__ void load_frag(const uint2* frag, uint2* s_frag) {
-  for (int i = threadIdx.x; i < kFrag; i += kThreads) s_frag[i] = frag[i];
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n"
+               :: "r"(tc05::smem_addr(mbar)) : "memory");
 }
 
 /* ------------------------------------------------------------ phase P */
@@ -305,67 +239,202 @@ struct ZSums {
   float rr, rz, zw;
 };
 
-/* One tile of phase Z. kFused: r_new = r_old - alpha w is written to rnew
- * and the dot products are accumulated; otherwise (the stand-alone
- * application) z = M^-1 r only. */
-template <bool kFused>
-__device__ __forceinline__ void phase_z_tile(int H, int W, int tile, int tiles_x,
-                                             const float* __restrict__ rold,
-                                             float* __restrict__ rnew,
-                                             const float* __restrict__ w,
-                                             const float* __restrict__ s,
-                                             float* __restrict__ z,
-                                             float alpha, float sigma, float zscale,
-                                             __half* s_y, const uint2* s_frag, ZSums& sums) {
-  const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
-  const int y0 = ty * kTH, x0 = tx * kTW;
-  stage_tile(H, W, y0, x0, rold, kFused ? w : nullptr, s, alpha, sigma, s_y);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = (warp / kWarpsX) * 16, wc = (warp % kWarpsX) * 32;
-  float acc[4][4];
-  stencil_mma(s_y, s_frag, wr, wc, acc);
-  const int g = lane >> 2, t = lane & 3;
+struct ZArgs {
+  int H, W, tiles_x, tiles;
+  const float* rold;
+  float* rnew;
+  const float* w;
+  const float* s;
+  float* z;
+  float alpha, sigma, zscale;
+};
+
+/* Per-block tcgen05 state. The counters are kept by the threads that wait on
+ * each mbarrier, so that every wait names the parity of the phase it needs. */
+struct TileState {
+  unsigned char* smem;
+  uint64_t* a_full;    /* [2] staged tile b is in shared memory (1 arrival) */
+  uint64_t* mma_done;  /* [2] the MMAs of buffer b completed (tcgen05.commit) */
+  uint64_t* d_free;    /* [2] accumulators of buffer b moved out (8 arrivals) */
+  uint64_t* drain;     /* every MMA issued so far completed (teardown) */
+  uint32_t tmem;
+  uint32_t a_uses[2], d_uses[2], issues[2];  /* issuer */
+  uint32_t done_uses[2];                     /* readers */
+};
+
+/* Stages y = sigma * s * (r - alpha w) for tile rows y0-8 .. y0+135 and
+ * columns x0-8 .. x0+71 as FP16 into the A buffer (zero outside the domain;
+ * W % 4 == 0, so a group of four columns is entirely inside or outside).
+ * Each thread issues the loads of two groups before it converts them. */
+__device__ __forceinline__ void stage_a(const ZArgs& A, int y0, int x0, unsigned char* abuf,
+                                        int tid, int nthr) {
+  constexpr int kTotal = kRows * kGroups;
+  for (int q0 = tid; q0 < kTotal; q0 += 2 * nthr) {
+    float4 r[2], ww[2], ss[2];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int gy = y0 + wr + g + 8 * h, gx = x0 + wc + 8 * j + 2 * t;
-      if (gy >= H || gx >= W) continue;
-      const size_t i = (size_t)gy * W + gx;
-      float2 rn = ld2(rold + i);
-      float2 ww = make_float2(0.f, 0.f);
-      if (kFused) {
-        ww = ld2(w + i);
-        rn.x -= alpha * ww.x;
-        rn.y -= alpha * ww.y;
-      }
-      const float2 ss = __ldg(reinterpret_cast<const float2*>(s + i));
-      const float2 zv = make_float2(ss.x * (acc[j][2 * h] * zscale) + ss.x * ss.x * rn.x,
-                                    ss.y * (acc[j][2 * h + 1] * zscale) + ss.y * ss.y * rn.y);
-      *reinterpret_cast<float2*>(z + i) = zv;
-      if (kFused) {
-        *reinterpret_cast<float2*>(rnew + i) = rn;
-        sums.rr += rn.x * rn.x + rn.y * rn.y;
-        sums.rz += rn.x * zv.x + rn.y * zv.y;
-        sums.zw += zv.x * ww.x + zv.y * ww.y;
+    for (int u = 0; u < 2; ++u) {
+      const int q = q0 + u * nthr;
+      const int row = q / kGroups, grp = q - row * kGroups;
+      const int gy = y0 - kHalo + row, gx = x0 - kHalo + 4 * grp;
+      r[u] = ww[u] = ss[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (q < kTotal && gy >= 0 && gy < A.H && gx >= 0 && gx < A.W) {
+        const size_t i = (size_t)gy * A.W + gx;
+        r[u] = ld4(A.rold + i);
+        if (A.w) ww[u] = ld4(A.w + i);
+        ss[u] = __ldg(reinterpret_cast<const float4*>(A.s + i));
       }
     }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int q = q0 + u * nthr;
+      if (q >= kTotal) break;
+      const int row = q / kGroups, grp = q - row * kGroups;
+      const float a = A.alpha, sg = A.sigma;
+      const __half2 lo = __floats2half2_rn(sg * ss[u].x * (r[u].x - a * ww[u].x),
+                                           sg * ss[u].y * (r[u].y - a * ww[u].y));
+      const __half2 hi = __floats2half2_rn(sg * ss[u].z * (r[u].z - a * ww[u].z),
+                                           sg * ss[u].w * (r[u].w - a * ww[u].w));
+      uint2 packed;
+      packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+      packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+      *reinterpret_cast<uint2*>(abuf + (grp >> 1) * kChunkBytes + row * 16 + (grp & 1) * 8) =
+          packed;
+    }
   }
-  __syncthreads();
+}
+
+/* The 85 MMAs of one tile (one thread): input window w (staged columns
+ * 16 w .. 16 w + 15, K-major chunks 2 w and 2 w + 1) at row offset
+ * dy = dyi - 8 reaches the 32 output columns 16 w - 16 .. 16 w + 15; even
+ * and odd windows accumulate into separate column ranges of the buffer, so
+ * every window's first MMA (dyi = 0) initialises its own columns. */
+__device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uint32_t d_tmem) {
+  const uint64_t a_desc = tc05::smem_desc(a_addr, kChunkBytes, 128);
+  const uint64_t b_desc = tc05::smem_desc(b_addr, 512, 128);
+#pragma unroll 1
+  for (int w = 0; w < kWindows; ++w) {
+    const uint32_t d = d_tmem + ((w & 1) ? 96u + 16u * (uint32_t)(w - 1) : 16u * (uint32_t)w);
+#pragma unroll 1
+    for (int dyi = 0; dyi < 17; ++dyi) {
+      const uint32_t aoff = (uint32_t)(2 * w * kChunkBytes + dyi * 16) >> 4;
+      const uint32_t boff = (uint32_t)(dyi * 1024) >> 4;
+      tc05::mma_f16(d, a_desc + aoff, b_desc + boff, kIdesc, dyi != 0);
+    }
+  }
+}
+
+/* Phase Z, warp 0: for each tile, wait until it is staged and its
+ * accumulator buffer has been read out, then issue its MMAs (lane 0) and
+ * commit them to mma_done. The whole warp runs the loop so that it reaches
+ * the block-wide barriers after the phase converged. */
+__device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int* status) {
+  const int lane = threadIdx.x & 31;
+  int j = 0;
+  for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
+    const int b = j & 1;
+    bool ok = tc05::mbar_wait(&T.a_full[b], T.a_uses[b] & 1u, kWaitNs);
+    T.a_uses[b]++;
+    if (ok && T.issues[b] > 0) {
+      ok = tc05::mbar_wait(&T.d_free[b], (T.issues[b] - 1u) & 1u, kWaitNs);
+    }
+    if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
+    __syncwarp();
+    if (lane == 0) {
+      tc05::fence_after_sync();
+      if (ok) {
+        issue_tile(tc05::smem_addr(T.smem + (b ? kOffA1 : kOffA0)),
+                   tc05::smem_addr(T.smem + kOffB), T.tmem + (uint32_t)b * kDCols);
+      }
+      tc05::mma_commit(&T.mma_done[b]);
+    }
+    T.issues[b]++;
+    __syncwarp();
+  }
+}
+
+/* Phase Z, warps 1..31: stage tile j, then finish tile j - 1: warps 4..11
+ * wait for its MMAs and move the accumulators (even + odd windows) to the
+ * row-major hand-over tile, and all workers write r_new = r_old - alpha w
+ * and z = s K y / sigma + s^2 r_new with coalesced accesses. */
+__device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
+                                               int* status) {
+  const int tid = threadIdx.x - 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool reader = warp >= 4 && warp < 4 + kReaders;
+  float* zt = reinterpret_cast<float*>(T.smem + kOffZ);
+  auto finish = [&](int tile, int bb) {
+    if (reader) {
+      const bool ok = tc05::mbar_wait(&T.mma_done[bb], T.done_uses[bb] & 1u, kWaitNs);
+      T.done_uses[bb]++;
+      if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
+      tc05::fence_after_sync();
+      const int sp = warp & 3, half = (warp - 4) >> 2;
+      const uint32_t base = T.tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)bb * kDCols +
+                            (uint32_t)(32 * half);
+      float* zr = zt + (32 * sp + lane) * kZStride + 32 * half;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        float ev[16], od[16];
+        tc05::tmem_ld16(base + 16 + 16 * q, ev);       /* even windows: 16 + c */
+        tc05::tmem_ld16(base + 96 + 16 * q, od);       /* odd windows: 96 + c */
+#pragma unroll
+        for (int i = 0; i < 16; ++i) zr[16 * q + i] = ev[i] + od[i];
+      }
+      tc05::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&T.d_free[bb]);
+    }
+    named_sync(kBarWorkers, kWorkers);
+    const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+    const int y0 = ty * kTH, x0 = tx * kTW;
+    constexpr int kQuads = kTH * kTW / 4;
+    for (int q = tid; q < kQuads; q += kWorkers) {
+      const int row = q / (kTW / 4), c4 = 4 * (q % (kTW / 4));
+      const int gy = y0 + row, gx = x0 + c4;
+      if (gy >= A.H || gx >= A.W) continue;
+      const size_t i = (size_t)gy * A.W + gx;
+      float4 rn = ld4(A.rold + i);
+      const float4 ww = ld4(A.w + i);
+      rn.x -= A.alpha * ww.x; rn.y -= A.alpha * ww.y;
+      rn.z -= A.alpha * ww.z; rn.w -= A.alpha * ww.w;
+      const float4 ss = __ldg(reinterpret_cast<const float4*>(A.s + i));
+      const float4 acc = *reinterpret_cast<const float4*>(zt + row * kZStride + c4);
+      float4 zv;
+      zv.x = ss.x * (acc.x * A.zscale) + ss.x * ss.x * rn.x;
+      zv.y = ss.y * (acc.y * A.zscale) + ss.y * ss.y * rn.y;
+      zv.z = ss.z * (acc.z * A.zscale) + ss.z * ss.z * rn.z;
+      zv.w = ss.w * (acc.w * A.zscale) + ss.w * ss.w * rn.w;
+      *reinterpret_cast<float4*>(A.z + i) = zv;
+      *reinterpret_cast<float4*>(A.rnew + i) = rn;
+      sums.rr += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
+      sums.rz += rn.x * zv.x + rn.y * zv.y + rn.z * zv.z + rn.w * zv.w;
+      sums.zw += zv.x * ww.x + zv.y * ww.y + zv.z * ww.z + zv.w * ww.w;
+    }
+  };
+  int prev = -1, prev_b = 0, j = 0;
+  for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
+    const int tile = A.tiles - 1 - c;
+    const int b = j & 1;
+    const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+    stage_a(A, ty * kTH, tx * kTW, T.smem + (b ? kOffA1 : kOffA0), tid, kWorkers);
+    tc05::fence_proxy_async_smem();
+    named_sync(kBarWorkers, kWorkers);
+    if (tid == 0) mbar_arrive(&T.a_full[b]);
+    if (prev >= 0) finish(prev, prev_b);
+    prev = tile;
+    prev_b = b;
+  }
+  if (prev >= 0) finish(prev, prev_b);
 }
 
 /* ----------------------------------------------------- persistent FPCG */
 
-__global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams P) {
-  __shared__ __align__(16) __half s_y[kRows * kStride];
-  __shared__ __align__(16) uint2 s_frag[kFrag];
-  __shared__ float s_red[kThreads / 32];
-  __shared__ double s_one;
+/* The solve; returns when done or when a wait ran out (status set). */
+__device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, float* s_red,
+                                          double* s_one) {
   const int G = gridDim.x;
   const int H = P.H, W = P.W;
   const double n = (double)H * (double)W;
-  load_frag(P.frag, s_frag);
   const float zscale_k = 1.0f / __ldg(P.kscale);
   double* part_pw = P.part;
   double* part_rr = P.part + G;
@@ -385,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams
     if (threadIdx.x == 0) part_rr[blockIdx.x] = (double)rr;
   }
   if (!tl_grid_barrier(P.sync, P.status)) return;
-  double rr = sum_partials(part_rr, G, &s_one);
+  double rr = sum_partials(part_rr, G, s_one);
   const double rr0 = rr;
   double rz_old = 0.0, alpha = 0.0, beta = 0.0;
   int par_r = 0, par_p = 0, iters = 0;
@@ -402,19 +471,19 @@ __global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams
       pw = block_sum(pw, s_red);
       if (threadIdx.x == 0) part_pw[blockIdx.x] = (double)pw;
       if (!tl_grid_barrier(P.sync, P.status)) return;
-      const double pwsum = sum_partials(part_pw, G, &s_one);
+      const double pwsum = sum_partials(part_pw, G, s_one);
       alpha = rz_old / pwsum;
     }
     /* ---- phase Z (step 0: z0 = M^-1 r0, alpha = 0) */
-    const float sigma = (float)(1.0 / sqrt(rr / n));
-    const float zscale = zscale_k / sigma;
-    const float af = (float)alpha;
+    ZArgs A;
+    A.H = H; A.W = W; A.tiles_x = P.tiles_x; A.tiles = P.tiles;
+    A.rold = rcur; A.rnew = rnext; A.w = P.w; A.s = P.s; A.z = P.z;
+    A.alpha = (float)alpha;
+    A.sigma = (float)(1.0 / sqrt(rr / n));
+    A.zscale = zscale_k / A.sigma;
     ZSums sums = {0.0f, 0.0f, 0.0f};
-    for (int c = blockIdx.x; c < P.tiles; c += G) {
-      const int tile = P.tiles - 1 - c;
-      phase_z_tile<true>(H, W, tile, P.tiles_x, rcur, rnext, P.w, P.s, P.z, af, sigma, zscale,
-                         s_y, s_frag, sums);
-    }
+    if (threadIdx.x < 32) z_issuer_warp(A, T, P.status);
+    else z_worker_warps(A, T, sums, P.status);
     const float t_rr = block_sum(sums.rr, s_red);
     const float t_rz = block_sum(sums.rz, s_red);
     const float t_zw = block_sum(sums.zw, s_red);
@@ -424,9 +493,9 @@ __global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams
       part_zw[blockIdx.x] = (double)t_zw;
     }
     if (!tl_grid_barrier(P.sync, P.status)) return;
-    rr = sum_partials(part_rr, G, &s_one);
-    const double rz = sum_partials(part_rz, G, &s_one);
-    const double zw = sum_partials(part_zw, G, &s_one);
+    rr = sum_partials(part_rr, G, s_one);
+    const double rz = sum_partials(part_rz, G, s_one);
+    const double zw = sum_partials(part_zw, G, s_one);
     beta = (k == 0) ? 0.0 : -alpha * zw / rz_old;
     rz_old = rz;
     par_r ^= 1;
@@ -452,6 +521,57 @@ __global__ void __launch_bounds__(kThreads, kBlocksPerSM) lpcg_kernel(LpcgParams
     *P.rr_out = rr;
   }
 }
+
+__global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ float s_red[kThreads / 32];
+  __shared__ double s_one;
+  TileState T;
+  T.smem = smem;
+  T.a_full = reinterpret_cast<uint64_t*>(smem + kOffBar);
+  T.mma_done = T.a_full + 2;
+  T.d_free = T.a_full + 4;
+  T.drain = T.a_full + 6;
+  for (int b = 0; b < 2; ++b) T.a_uses[b] = T.d_uses[b] = T.issues[b] = T.done_uses[b] = 0;
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kOffTmem);
+  if (threadIdx.x < 32) {
+    tc05::tmem_alloc(s_tmem, kTmemCols);
+    tc05::tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b) {
+      tc05::mbar_init(&T.a_full[b], 1);
+      tc05::mbar_init(&T.mma_done[b], 1);
+      tc05::mbar_init(&T.d_free[b], kReaders);
+    }
+    tc05::mbar_init(T.drain, 1);
+    tc05::mbar_fence_init();
+  }
+  for (int i = threadIdx.x; i < kBBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(smem + kOffB)[i] = reinterpret_cast<const uint4*>(P.umma)[i];
+  tc05::fence_proxy_async_smem();
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  T.tmem = *s_tmem;
+
+  lpcg_body(P, T, s_red, &s_one);
+
+  /* Teardown: every MMA this block issued has completed (a commit tracks all
+   * of the issuing thread's earlier MMAs), then the tensor memory is freed. */
+  if (threadIdx.x == 0) {
+    tc05::mma_commit(T.drain);
+    if (!tc05::mbar_wait(T.drain, 0, kWaitNs)) atomicCAS(P.status, 0, TL_ERR_TIMEOUT);
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc05::fence_after_sync();
+    tc05::tmem_dealloc(T.tmem, kTmemCols);
+  }
+}
+
+
 
 /* ------------------------------------------- stand-alone application */
 
@@ -648,8 +768,9 @@ int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* 
  * FP32 arrays: solves A32 e = r until r.r <= tol^2 r0.r0 or max_iters steps.
  * r is the incoming residual (the kernel leaves the final residual in r or
  * r_alt); e, w, z, pa, pb are scratch of H*W floats, all 16-byte aligned.
- * The step count and the final r.r land in the pinned result page. */
-int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* kscale, int H,
+ * umma: the window B operands of the network's stencil. Returns the step
+ * count and the final r.r. */
+int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
                                int W, const float* kx, const float* ky, const float* s,
                                float* r, float* r_alt, float* e, float* w, float* z, float* pa,
                                float* pb, double tol, int max_iters, int* iters,
@@ -659,11 +780,12 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* k
   TL_REQUIRE(max_iters >= 0 && tol > 0.0, "tl_internal_fpcg_collapsed: bad arguments");
   const size_t n = (size_t)H * W;
   const void* kernel = (const void*)lpcg_kernel;
+  TL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kLpcgSmem));
   int per_sm = 0;
-  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0));
+  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, kLpcgSmem));
   TL_REQUIRE(per_sm >= 1, "the learned PCG kernel cannot be resident");
-  per_sm = std::min(per_sm, kBlocksPerSM);
-  const int G = per_sm * ctx->num_sms;
+  /* one block per SM: each block holds all 512 tensor-memory columns */
+  const int G = ctx->num_sms;
   rc = tl_ensure_partials(ctx, (size_t)G);
   if (rc != TL_OK) return rc;
   TL_CUDA(cudaMemsetAsync(e, 0, n * sizeof(float), ctx->stream));
@@ -688,7 +810,7 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* k
   P.z = z;
   P.p0 = pa;
   P.p1 = pb;
-  P.frag = reinterpret_cast<const uint2*>(frag);
+  P.umma = reinterpret_cast<const __half*>(umma);
   P.kscale = kscale;
   P.part = ctx->d_part;
   P.sync = ctx->d_sync;
@@ -700,13 +822,15 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* frag, const float* k
   TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   ctx->h_steps[0] = -1;
   void* args[] = {&P};
-  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(kThreads), args, 0, ctx->stream));
+  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(kThreads), args, kLpcgSmem,
+                                      ctx->stream));
   TL_CHECK_LAUNCH(ctx);
   int status = 0;
   TL_CUDA(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
                           ctx->stream));
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (status != 0) return tl_set_error(status, "learned PCG kernel: grid-barrier timeout");
+  if (status != 0)
+    return tl_set_error(status, "learned PCG kernel: a grid-barrier or MMA wait timed out");
   *iters = ((volatile int*)ctx->h_steps)[0];
   *rr_final = ((volatile double*)ctx->h_result)[7];
   return TL_OK;
