@@ -11,6 +11,7 @@
 typedef double* FieldBufferType;
 
 struct tl_context;
+struct tl_net;
 
 typedef struct ChunkExtension {
   struct tl_context* ctx;
@@ -26,4 +27,6 @@ typedef struct ChunkExtension {
   int replace_method;     /* -1, or a TL_METHOD_* that replaces the CG solve */
   double replace_rel_tol; /* its relative FP64 true-residual target */
   double replace_inner_tol;
+  struct tl_net* net;     /* the learned preconditioner (mixed-learned) */
+  int fp64_fused;         /* 1: fused multiply-add contract of the FP64 CG */
 } ChunkExtension;

@@ -30,8 +30,10 @@
  * fails.
  *
  * Solver replacement. With the deck key `gb300_solver <cg64|mixed|
- * mixed-jacobi>` (or TL_SOLVER in the environment; `preconditioner_on`
- * alone selects mixed-jacobi), run_cg_init solves the timestep with
+ * mixed-jacobi|mixed-learned>` (or TL_SOLVER in the environment;
+ * `preconditioner_on` alone selects mixed-jacobi; mixed-learned reads the
+ * network's weights from `gb300_weights <file>` or TL_WEIGHTS: raw
+ * little-endian FP32, tl_net_num_params() values), run_cg_init solves the timestep with
  * tl_solve to a relative FP64 true residual (`gb300_rel_tol`, default
  * 1e-10; `gb300_inner_tol`, default 1e-5) and then reports rro = pw = 1,
  * rrn = 0, so that the driver's CG loop ends after one pass and prints
@@ -39,8 +41,13 @@
  * residual on a TL_SOLVE line. The reference driver ignores the gb300_* keys
  * (TeaLeaf/parse_config.c:77-192 skips unknown lines).
  *
+ * FP64 arithmetic. `gb300_fp64 fused` (or TL_FP64=fused) selects the fused
+ * multiply-add contract of the persistent FP64 CG (tl_set_fp64_contract);
+ * the default, exact, is bit-identical to the reference's C kernels.
+ *
  * Environment: TL_DEVICE (GPU index, default 0), TL_CG_MODE ("fused", the
- * default, or "stepwise"), TL_SOLVER (as gb300_solver), TL_PRINT_SUMMARY=1
+ * default, or "stepwise"), TL_SOLVER (as gb300_solver), TL_WEIGHTS (as
+ * gb300_weights), TL_FP64 (as gb300_fp64), TL_PRINT_SUMMARY=1
  * (print the four field-summary sums at full precision), TL_PRINT_SOLVE=1
  * (print per-solve device steps), TL_DUMP_DIR=<dir> (write density, energy
  * and u as VisIt BOV files at every field summary).
@@ -79,9 +86,38 @@ static int method_from_name(const char* name) {
   if (strcmp(name, "cg64") == 0) return TL_METHOD_CG64;
   if (strcmp(name, "mixed") == 0) return TL_METHOD_MIXED_CG;
   if (strcmp(name, "mixed-jacobi") == 0) return TL_METHOD_MIXED_JACOBI;
+  if (strcmp(name, "mixed-learned") == 0) return TL_METHOD_MIXED_LEARNED;
   if (strcmp(name, "cg") == 0 || strcmp(name, "reference") == 0) return -1;
   die(__LINE__, __FILE__, "GB300 backend: unknown solver '%s'\n", name);
   return -1;
+}
+
+static int fp64_from_name(const char* name) {
+  if (strcmp(name, "exact") == 0) return 0;
+  if (strcmp(name, "fused") == 0) return 1;
+  die(__LINE__, __FILE__, "GB300 backend: unknown FP64 contract '%s'\n", name);
+  return 0;
+}
+
+/* The learned preconditioner's weights: a raw little-endian FP32 file of
+ * tl_net_num_params() values. */
+static void load_network(ChunkExtension* ext, const char* path) {
+  if (!path || !*path) {
+    die(__LINE__, __FILE__,
+        "GB300 backend: mixed-learned needs the weights file (gb300_weights or TL_WEIGHTS)\n");
+  }
+  const int n = tl_net_num_params();
+  std::vector<float> w((size_t)n);
+  FILE* f = fopen(path, "rb");
+  if (!f) die(__LINE__, __FILE__, "GB300 backend: cannot open weights file %s\n", path);
+  const size_t got = fread(w.data(), sizeof(float), (size_t)n, f);
+  const bool extra = fgetc(f) != EOF;
+  fclose(f);
+  if (got != (size_t)n || extra) {
+    die(__LINE__, __FILE__, "GB300 backend: %s does not hold %d FP32 weights\n", path, n);
+  }
+  TL_TRY(tl_net_create(ext->ctx, &ext->net), "network creation");
+  TL_TRY(tl_net_set_weights(ext->net, w.data(), n), "network weights");
 }
 
 /* The backend's own deck keys (gb300_*), read from the same tea.in. */
@@ -89,6 +125,8 @@ static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
   ext->replace_method = settings->preconditioner ? TL_METHOD_MIXED_JACOBI : -1;
   ext->replace_rel_tol = 1e-10;
   ext->replace_inner_tol = 1e-5;
+  ext->fp64_fused = 0;
+  char weights[512] = "";
   FILE* f = fopen(settings->tea_in_filename, "r");
   if (f) {
     char line[512], word[128];
@@ -97,11 +135,21 @@ static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
       if (sscanf(line, " gb300_solver %127s", word) == 1) ext->replace_method = method_from_name(word);
       if (sscanf(line, " gb300_rel_tol %lf", &v) == 1) ext->replace_rel_tol = v;
       if (sscanf(line, " gb300_inner_tol %lf", &v) == 1) ext->replace_inner_tol = v;
+      if (sscanf(line, " gb300_fp64 %127s", word) == 1) ext->fp64_fused = fp64_from_name(word);
+      char path[512];
+      if (sscanf(line, " gb300_weights %511s", path) == 1) snprintf(weights, sizeof(weights), "%s", path);
     }
     fclose(f);
   }
   const char* env = getenv("TL_SOLVER");
   if (env) ext->replace_method = method_from_name(env);
+  env = getenv("TL_FP64");
+  if (env) ext->fp64_fused = fp64_from_name(env);
+  env = getenv("TL_WEIGHTS");
+  if (env) snprintf(weights, sizeof(weights), "%s", env);
+  TL_TRY(tl_set_fp64_contract(ext->ctx, ext->fp64_fused ? TL_FP64_FUSED : TL_FP64_EXACT),
+         "FP64 contract");
+  if (ext->replace_method == TL_METHOD_MIXED_LEARNED) load_network(ext, weights);
 }
 
 /* TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:31-80 */
@@ -168,6 +216,8 @@ void run_kernel_finalise(Chunk* chunk, Settings* settings) {
   free(chunk->cheby_betas);
   free(ext->ra_pw);
   free(ext->ra_rrn);
+  if (ext->net) TL_TRY(tl_net_destroy(ext->net), "network release");
+  ext->net = NULL;
   TL_TRY(tl_context_destroy(ext->ctx), "context release");
   ext->ctx = NULL;
 }
@@ -298,7 +348,9 @@ void run_cg_init(Chunk* chunk, Settings* settings, double rx, double ry,
   ChunkExtension* ext = chunk->ext;
   if (ext->replace_method >= 0 && settings->solver == CG_SOLVER) {
     tl_solve_params prm;
+    memset(&prm, 0, sizeof(prm));
     prm.method = ext->replace_method;
+    prm.learned = ext->net;
     prm.rel_tol = ext->replace_rel_tol;
     prm.inner_tol = ext->replace_inner_tol;
     prm.max_inner = settings->max_iters;

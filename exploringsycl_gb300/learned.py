@@ -29,6 +29,7 @@ LAYOUT_VERSION = 1
 N_LAYERS = 4
 CH = 16
 DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "weights" / "precond_4x16.npz"
+DEFAULT_RAW_WEIGHTS = DEFAULT_WEIGHTS.with_suffix(".f32")
 
 
 def num_params() -> int:
@@ -62,6 +63,14 @@ def save_weights(path: str | Path, w: np.ndarray, meta: dict | None = None) -> P
     p.parent.mkdir(parents=True, exist_ok=True)
     np.savez(p, weights=w, version=np.int32(LAYOUT_VERSION), sha256=np.array(digest),
              meta=np.array(json.dumps(meta or {})))
+    return p
+
+
+def export_raw(w: np.ndarray, path: str | Path = DEFAULT_RAW_WEIGHTS) -> Path:
+    """Writes the weights as the raw little-endian FP32 file that the run_*
+    backend reads (deck key gb300_weights, or TL_WEIGHTS)."""
+    p = Path(path)
+    np.ascontiguousarray(w, dtype="<f4").tofile(p)
     return p
 
 

@@ -46,13 +46,16 @@ def test_tabulated_temperature(n, steps, tmp_path, backend_built):
     assert run.passed is True, run.stdout[-800:]
 
 
-@pytest.mark.parametrize("solver", ["cg64", "mixed", "mixed-jacobi"])
+@pytest.mark.parametrize("solver", ["cg64", "mixed", "mixed-jacobi", "mixed-learned"])
 def test_solver_replacement_under_the_driver(solver, tmp_path, backend_built, oracle_built):
     """gb300_solver in the deck: the driver loop ends after one pass, the
     backend reports the true solve, and the final temperature agrees with
-    the oracle's plain CG (absolute eps 1e-15) to 1e-8."""
+    the oracle's plain CG (absolute eps 1e-15) to 1e-8. mixed-learned reads
+    the committed weights through gb300_weights."""
+    from exploringsycl_gb300.learned import DEFAULT_RAW_WEIGHTS
     d = dk.two_state(96, end_step=2)
-    d.extra = [f"gb300_solver {solver}", "gb300_rel_tol 1e-11"]
+    d.extra = [f"gb300_solver {solver}", "gb300_rel_tol 1e-11",
+               f"gb300_weights {DEFAULT_RAW_WEIGHTS}"]
     gpu = run_driver(DRIVER_EXE, d, tmp_path / "gpu")
     cpu = run_driver(oracle_built.DRIVER, d, tmp_path / "cpu")
     assert gpu.returncode == 0, gpu.stdout[-2000:]
@@ -89,3 +92,19 @@ def test_gpu_driver_matches_reference_driver_golden(name, tmp_path, backend_buil
     assert r.errors == g["errors"]
     assert [list(s) for s in r.summaries] == g["summaries"]
     assert r.passed == g["passed"]
+
+
+def test_fused_fp64_contract_under_the_driver(tmp_path, backend_built):
+    """gb300_fp64 fused: the same decks through the driver with the fused
+    multiply-add CG; iteration counts within one of the exact contract's and
+    every field summary within 1e-10 relative."""
+    d = dk.five_state(64, end_step=3)
+    exact = run_driver(DRIVER_EXE, d, tmp_path / "exact")
+    d.extra = ["gb300_fp64 fused"]
+    fused = run_driver(DRIVER_EXE, d, tmp_path / "fused")
+    assert exact.returncode == 0 and fused.returncode == 0, fused.stdout[-2000:]
+    assert len(exact.iterations) == len(fused.iterations) == 3
+    assert all(abs(a - b) <= 1 for a, b in zip(exact.iterations, fused.iterations))
+    for se, sf in zip(exact.summaries, fused.summaries):
+        for a, b in zip(se, sf):
+            assert abs(a - b) <= 1e-10 * abs(a)

@@ -84,3 +84,11 @@ def test_collapsed_operator_is_symmetric_positive_definite():
     assert np.allclose(M, M.T, rtol=0, atol=1e-12 * np.abs(M).max())
     ev = np.linalg.eigvalsh(0.5 * (M + M.T))
     assert ev.min() >= 0.99 * (s ** 2).min()
+
+
+def test_raw_weights_file_matches_the_npz():
+    """The raw FP32 file the run_* backend reads holds the committed weights."""
+    from exploringsycl_gb300.learned import DEFAULT_RAW_WEIGHTS, DEFAULT_WEIGHTS, load_weights
+    w, _ = load_weights(DEFAULT_WEIGHTS)
+    raw = np.fromfile(DEFAULT_RAW_WEIGHTS, dtype="<f4")
+    assert raw.shape == w.shape and np.array_equal(raw, w)
