@@ -75,7 +75,7 @@ NCU_BYTES_PER_CELL_STEP = {
     ("cg_persistent_kernel", "exact"): 115.4,  # profiles/cg_persistent_fp64_exact_4096.txt
     ("cg_persistent_kernel", "fused"): 120.1,  # profiles/cg_persistent_fp64_fused_4096.txt
     ("inner_cg_kernel", None): 51.3,           # profiles/inner_cg_mixed_jacobi_4096.txt
-    ("lpcg_kernel", None): 50.6,               # profiles/lpcg_learned_4096.txt
+    ("lpcg_kernel", None): 51.3,               # profiles/lpcg_learned_4096.txt
 }
 ITER_FIXTURES = {"two-state": ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json",
                  "random": ROOT / "tests" / "golden" / "cg_iterations_random_4096.json"}
