@@ -107,8 +107,7 @@ int tl_internal_fpcg_learned(tl_context* ctx, tl_net* net, int H, int W, const f
                              const float* ky, const float* s, float* r, float* e, float* p,
                              float* w, float* z, double tol, int max_iters, int* iters);
 /* The learned preconditioner collapsed to one stencil (tl_precond.cu). */
-int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
-                            const float** kscale);
+int tl_internal_net_stencil(tl_net* net, const void** umma, const float** kscale);
 int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,
                                 int W, const float* r, const float* s, float* z);
 int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* kscale, int H,

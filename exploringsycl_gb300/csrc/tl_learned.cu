@@ -472,18 +472,15 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
 /* ----------------------------------------------- collapse to a stencil */
 
 constexpr int kStencil = 17;            /* C^T C: 17 x 17 taps */
-constexpr int kFragEntries = 17 * 2 * 2 * 32;
 constexpr int kUmmaHalves = 17 * 2 * 256;  /* 34 B operands of 16 x 16 FP16 */
 constexpr int kUmma32Halves = 17 * 512;    /* 17 B operands of 32 x 16 FP16 */
 
 /* Composes the four layers into the 16-channel 9x9 kernel G of C (G(u)
  * multiplies the input at offset u), then K(d) = sum_u G(u).G(u + d), the
- * stencil of C^T C, and the tensor-core B fragments of its banded Toeplitz
- * blocks (tl_precond.cu): entry [dy][par][kb][lane] holds
- * T(k, n) = K(dy, 16 kb + k - 8 - 8 par - n) for k = 2t, 2t+1 and 2t+8, 2t+9,
- * n = g (lane = 4 g + t), as FP16 pairs, K scaled by kscale = 2^-ceil(log2 max|K|).
- * umma holds the same Toeplitz blocks as tcgen05 B operands: matrix
- * (dy, kb) at halves 256 (2 dy + kb), element (n, k) = T(k, n) at
+ * stencil of C^T C, and the tcgen05 B operands of its banded Toeplitz blocks
+ * (tl_precond.cu), as FP16, K scaled by kscale = 2^-ceil(log2 max|K|).
+ * umma (stand-alone application, N = 16) holds matrix (dy, kb) at halves
+ * 256 (2 dy + kb), element (n, k) = K(dy, 16 kb + k - 8 - n) at
  * (k / 8) 128 + 8 n + k % 8 (K-major core matrices, 16 x 16). umma32 holds,
  * per dy, the 32 x 16 operand of one 16-column input window and the 32
  * output columns it reaches: element (n, k) = K(dy, k + 8 - n) at halves
@@ -491,7 +488,6 @@ constexpr int kUmma32Halves = 17 * 512;    /* 17 B operands of 32 x 16 FP16 */
  * One block; runs whenever the weights change. */
 __global__ void __launch_bounds__(256) collapse_kernel(const float* __restrict__ master,
                                                         float* __restrict__ k_out,
-                                                        uint2* __restrict__ frag,
                                                         __half* __restrict__ umma,
                                                         __half* __restrict__ umma32,
                                                         float* __restrict__ kscale_out) {
@@ -556,17 +552,6 @@ __global__ void __launch_bounds__(256) collapse_kernel(const float* __restrict__
   auto tap = [&](int dy, int dx) -> float {
     return (dx < -8 || dx > 8) ? 0.0f : kscale * s_k[(dy + 8) * kStencil + dx + 8];
   };
-  for (int i = tid; i < kFragEntries; i += blockDim.x) {
-    const int lane = i & 31, kb = (i >> 5) & 1, par = (i >> 6) & 1, dyi = i >> 7;
-    const int g = lane >> 2, t = lane & 3, dy = dyi - 8;
-    const int base = 16 * kb - 8 - 8 * par - g;
-    const __half2 lo = __floats2half2_rn(tap(dy, base + 2 * t), tap(dy, base + 2 * t + 1));
-    const __half2 hi = __floats2half2_rn(tap(dy, base + 2 * t + 8), tap(dy, base + 2 * t + 9));
-    uint2 v;
-    v.x = *reinterpret_cast<const uint32_t*>(&lo);
-    v.y = *reinterpret_cast<const uint32_t*>(&hi);
-    frag[i] = v;
-  }
   for (int i = tid; i < kUmmaHalves; i += blockDim.x) {
     const int mat = i >> 8, e = i & 255;
     const int dyi = mat >> 1, kb = mat & 1;
@@ -614,7 +599,6 @@ struct tl_net {
   int sums_cap = 0;
   /* the network collapsed to its 17x17 stencil (collapse_kernel) */
   float* stencil_k = nullptr;     /* K, 289 floats */
-  uint2* stencil_frag = nullptr;  /* tensor-core fragments of K * kscale (FP16) */
   __half* stencil_umma = nullptr; /* the same as tcgen05 B operands */
   __half* stencil_umma32 = nullptr; /* window operands of N = 32 (persistent solve) */
   float* stencil_kscale = nullptr;
@@ -754,7 +738,7 @@ static int refresh_weights(tl_net* net) {
       net->master, net->fwd16, net->adj16, net->l1_fwd, net->l1_adj);
   TL_CHECK_LAUNCH(net->ctx);
   collapse_kernel<<<1, 256, 0, net->ctx->stream>>>(net->master, net->stencil_k,
-                                                    net->stencil_frag, net->stencil_umma,
+                                                    net->stencil_umma,
                                                     net->stencil_umma32, net->stencil_kscale);
   TL_CHECK_LAUNCH(net->ctx);
   return TL_OK;
@@ -1034,7 +1018,6 @@ extern "C" int tl_net_create(tl_context* ctx, tl_net** out) {
   if (e == cudaSuccess) e = cudaMalloc(&net->l1_adj, 9 * kCh * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&net->dadj, n16 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_k, kStencil * kStencil * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&net->stencil_frag, kFragEntries * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_umma, kUmmaHalves * sizeof(__half));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_umma32, kUmma32Halves * sizeof(__half));
   if (e == cudaSuccess) e = cudaMalloc(&net->stencil_kscale, sizeof(float));
@@ -1055,7 +1038,7 @@ extern "C" int tl_net_destroy(tl_net* net) {
   cudaFree(net->master); cudaFree(net->grad); cudaFree(net->adam_m); cudaFree(net->adam_v);
   cudaFree(net->fwd16); cudaFree(net->adj16); cudaFree(net->l1_fwd); cudaFree(net->l1_adj);
   cudaFree(net->dadj); cudaFree(net->partial);
-  cudaFree(net->stencil_k); cudaFree(net->stencil_frag); cudaFree(net->stencil_kscale);
+  cudaFree(net->stencil_k); cudaFree(net->stencil_kscale);
   cudaFree(net->stencil_umma);
   cudaFree(net->stencil_umma32);
   for (auto& a : net->act) cudaFree(a);
@@ -1142,10 +1125,8 @@ extern "C" int tl_net_apply_stencil(tl_net* net, int H, int W, const float* r, c
                                      s, z);
 }
 
-int tl_internal_net_stencil(tl_net* net, const void** frag, const void** umma,
-                            const float** kscale) {
-  TL_REQUIRE(net && frag && umma && kscale, "tl_internal_net_stencil: null argument");
-  *frag = net->stencil_frag;
+int tl_internal_net_stencil(tl_net* net, const void** umma, const float** kscale) {
+  TL_REQUIRE(net && umma && kscale, "tl_internal_net_stencil: null argument");
   *umma = net->stencil_umma32;
   *kscale = net->stencil_kscale;
   return TL_OK;

@@ -517,10 +517,9 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
           rc = tl_internal_fpcg_learned(ctx, prm->learned, H, W, kx32, ky32, invd, r32, e32, pa,
                                         w32, pb, tol, prm->max_inner, &it);
         } else {
-          const void* frag = nullptr;
           const void* umma = nullptr;
           const float* kscale = nullptr;
-          rc = tl_internal_net_stencil(prm->learned, &frag, &umma, &kscale);
+          rc = tl_internal_net_stencil(prm->learned, &umma, &kscale);
           if (rc != TL_OK) return rc;
           rc = tl_internal_fpcg_collapsed(ctx, umma, kscale, H, W, kx32, ky32, invd, r32, r32b,
                                           e32, w32, z32, pa, pb, tol, prm->max_inner, &it,

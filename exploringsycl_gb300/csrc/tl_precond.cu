@@ -15,43 +15,48 @@
  * the zero-extended field once instead of truncating every layer, so S K S
  * is a principal submatrix of a positive semi-definite Toeplitz operator and
  * M^-1 stays symmetric positive definite. Cost: 289 multiply-adds per cell
- * against ~28 k for the eight 16-channel layers. K and the fragment table
- * below are built on the device from the FP32 master weights whenever the
+ * against ~28 k for the eight 16-channel layers. K and its tensor-core
+ * operands are built on the device from the FP32 master weights whenever the
  * weights change (tl_learned.cu, collapse_kernel).
  *
- * Tensor cores. For a block of 16 output rows and one row offset dy, the
- * correlation along a row with K(dy, .) is a product with a banded Toeplitz
- * matrix: for 8 output columns starting at xc, the inputs xc-8 .. xc+15 form
- * two 16-column k-blocks, and
- *   Z[16 x 8] += Y[16 x 16] T0[16 x 8] + Y'[16 x 16] T1[16 x 8],
- * T(k, n) = K(dy, 16 kb + k - 8 - 8 par - n) (0 where |dx| > 8), with par the
- * parity of the 8-column block within its 16-column window. That is 34
- * mma.sync m16n8k16 (FP16 inputs, FP32 accumulation) per 128 outputs. A warp
- * owns 16 rows x 32 columns: per dy it loads three 16x16 data windows with
- * ldmatrix and four T fragments (the same for every tile, kept in shared
- * memory in fragment order) and issues 8 MMAs. The scaled residual y = S r is
- * staged in FP16 with its 8-cell halo, multiplied by sigma = 1 / RMS(r) so
- * that its values sit in FP16's normal range whatever the residual's size
- * (the operator is linear; the factor is removed in the epilogue); K is
- * scaled by a power of two for the same reason.
+ * Tensor cores (tcgen05). For one row offset dy, correlating a row with
+ * K(dy, .) is a product with a banded Toeplitz matrix. A 16-column input
+ * window reaches 32 output columns, so one MMA of M = 128 tile rows, N = 32,
+ * K = 16 (FP16 inputs, FP32 accumulation in tensor memory, lane = tile row)
+ * per window and dy: 85 per 128 x 64 tile, issued by one thread. The A
+ * operand is the staged y = sigma S r in the canonical K-major layout
+ * (tl_tc05.cuh): chunks of 8 staged columns, each 144 rows x 16 bytes, so a
+ * window is two consecutive chunks and the row offset dy a shift of the
+ * start address by 16 (dy + 8) bytes. sigma = 1 / RMS(r) keeps y in FP16's
+ * normal range whatever the residual's size (the operator is linear; the
+ * factor is removed in the epilogue), and K is scaled by a power of two for
+ * the same reason. The output ranges of neighbouring windows overlap, so
+ * even and odd windows accumulate into separate tensor-memory columns, and
+ * the epilogue adds the two.
  *
  * Flexible PCG (Polak-Ribiere beta = z_new.(r_new - r_old) / z_old.r_old,
  * r_new - r_old = -alpha w), on the packed interior [H][W] with zero-flux
- * edges, one cooperative persistent kernel, two phases and two grid barriers
- * per step:
- *   P: p_new = z + beta p_old at the cell and its four neighbours, w = A p_new,
- *      p.w partial sums (linear chunks of 2048 cells, float4 per thread), and
- *      the previous step's e += alpha p_old;
- *   Z: r_new = r_old - alpha w and y = sigma S r_new on a 64 x 128 tile and its
- *      halo (shared memory, FP16), z = S K y / sigma + D^-1 r_new on the tensor
- *      cores; partial sums of r.r, r.z and z.w.
+ * edges, one cooperative persistent kernel of one 1024-thread block per SM,
+ * two phases and two grid barriers per step:
+ *   P: (all warps) p_new = z + beta p_old at the cell and its four
+ *      neighbours, w = A p_new, p.w partial sums, and the previous step's
+ *      e += alpha p_old;
+ *   Z: warp 0 issues each tile's MMAs and commits them to an mbarrier;
+ *      warps 1..31 stage the next tile (r_new = r_old - alpha w and its
+ *      8-cell halo as y, FP16) into one of two shared buffers and finish the
+ *      previous tile: eight of them move its accumulators from tensor memory
+ *      into a row-major shared tile, and all of them write r_new and
+ *      z = S K y / sigma + D^-1 r_new with coalesced stores and sum r.r,
+ *      r.z and z.w. Staged tiles and accumulators are double-buffered, so
+ *      the tensor core works while the block streams memory.
  * The residual is double-buffered because a tile reads its neighbours' old
  * residual while they write the new one. Memory per cell and step: P reads z,
  * p_old, kx, ky, e and writes p_new, w, e (32 B); Z reads r, w, s and writes r,
  * z (20 B): 52 B, against 56 B for the Jacobi-PCG kernel of tl_mixed.cu. The
  * last step's e update is one extra pass at the end. Tiles of phase Z are
  * visited in reverse order so that the cells phase P wrote last are still in
- * L2.
+ * L2. Every mbarrier wait is bounded; tensor memory is freed after a final
+ * commit on every exit path.
  */
 #include <cuda_fp16.h>
 #include <math.h>

@@ -229,3 +229,24 @@ def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
             g.close()
     a, b = steps["mixed-learned"], steps["mixed-learned-layers"]
     assert abs(a - b) <= 0.05 * b, steps
+
+
+@pytest.mark.parametrize("nx,ny", [(132, 100), (68, 260), (8, 40), (260, 3)])
+def test_collapsed_fpcg_on_ragged_fields(nx, ny, backend_built):
+    """The persistent tcgen05 solve on interiors that leave ragged 128 x 64
+    tiles (and fields smaller than one tile, or than the 8-cell halo):
+    reaches the FP64 target without a fall-back, like the Jacobi solve."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
+    w, _ = load_weights(DEFAULT_WEIGHTS)
+    d = dk.Deck(nx, ny, dk.random_states(11), end_step=1)
+    g = GpuChunk(d)
+    net = Net(g.ctx, w)
+    try:
+        rep = g.solve_timestep("mixed-learned", rel_tol=1e-10, learned=net)
+        assert rep["final_rel_residual"] <= 1e-10, rep
+        assert rep["fallback_events"] == 0, rep
+        assert rep["inner_steps"] > 0
+    finally:
+        net.close()
+        g.close()
