@@ -23,7 +23,7 @@
  * K(dy, .) is a product with a banded Toeplitz matrix. A 16-column input
  * window reaches 32 output columns, so one MMA of M = 128 tile rows, N = 32,
  * K = 16 (FP16 inputs, FP32 accumulation in tensor memory, lane = tile row)
- * per window and dy: 85 per 128 x 64 tile, issued by one thread. The A
+ * per window and dy: 85 per 128 x 64 tile, issued by two threads. The A
  * operand is the staged y = sigma S r in the canonical K-major layout
  * (tl_tc05.cuh): chunks of 8 staged columns, each 144 rows x 16 bytes, so a
  * window is two consecutive chunks and the row offset dy a shift of the
@@ -41,8 +41,8 @@
  *   P: (all warps) p_new = z + beta p_old at the cell and its four
  *      neighbours, w = A p_new, p.w partial sums, and the previous step's
  *      e += alpha p_old;
- *   Z: warp 0 issues each tile's MMAs and commits them to an mbarrier;
- *      warps 1..31 stage the next tile (r_new = r_old - alpha w and its
+ *   Z: warps 0 and 1 issue each tile's MMAs (even and odd windows) and
+ *      commit them to mbarriers; warps 2..31 stage the next tile (r_new = r_old - alpha w and its
  *      8-cell halo as y, FP16) into one of two shared buffers and finish the
  *      previous tile: eight of them move its accumulators from tensor memory
  *      into a row-major shared tile, and all of them write r_new and
@@ -70,7 +70,8 @@
 namespace {
 
 constexpr int kThreads = 1024;          /* 32 warps, one block per SM */
-constexpr int kWorkers = kThreads - 32; /* phase Z: warps 1..31; warp 0 issues the MMAs */
+constexpr int kIssuers = 2;             /* phase Z: warps 0, 1 issue the MMAs */
+constexpr int kWorkers = kThreads - 32 * kIssuers;  /* warps 2..31 stage and finish tiles */
 constexpr int kChunk = 4 * kThreads;    /* phase P: cells per block iteration */
 constexpr int kHalo = 8;
 constexpr int kTH = 128;                /* tile rows = MMA M = tensor-memory lanes */
@@ -99,8 +100,9 @@ constexpr int kOffA0 = 0;
 constexpr int kOffA1 = kABuf;
 constexpr int kOffB = 2 * kABuf;
 constexpr int kOffZ = kOffB + kBBytes;
-constexpr int kOffBar = kOffZ + kTH * kZStride * 4;  /* a_full[2] mma_done[2] d_free[2] drain */
-constexpr int kOffTmem = kOffBar + 7 * 8;
+/* mbarriers: a_full[2], mma_done[2][kIssuers], d_free[2], drain */
+constexpr int kOffBar = kOffZ + kTH * kZStride * 4;
+constexpr int kOffTmem = kOffBar + (5 + 2 * kIssuers) * 8;
 constexpr int kLpcgSmem = (kOffTmem + 8 + 127) / 128 * 128;
 static_assert(kOffB % 128 == 0 && kOffZ % 16 == 0 && kOffBar % 8 == 0, "alignment");
 static_assert(2 * kDCols <= kTmemCols, "tensor memory");
@@ -259,7 +261,7 @@ struct ZArgs {
 struct TileState {
   unsigned char* smem;
   uint64_t* a_full;    /* [2] staged tile b is in shared memory (1 arrival) */
-  uint64_t* mma_done;  /* [2] the MMAs of buffer b completed (tcgen05.commit) */
+  uint64_t* mma_done;  /* [2][kIssuers] issuer i's MMAs of buffer b completed */
   uint64_t* d_free;    /* [2] accumulators of buffer b moved out (8 arrivals) */
   uint64_t* drain;     /* every MMA issued so far completed (teardown) */
   uint32_t tmem;
@@ -313,11 +315,12 @@ __device__ __forceinline__ void stage_a(const ZArgs& A, int y0, int x0, unsigned
  * dy = dyi - 8 reaches the 32 output columns 16 w - 16 .. 16 w + 15; even
  * and odd windows accumulate into separate column ranges of the buffer, so
  * every window's first MMA (dyi = 0) initialises its own columns. */
-__device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uint32_t d_tmem) {
+__device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uint32_t d_tmem,
+                                           int w0) {
   const uint64_t a_desc = tc05::smem_desc(a_addr, kChunkBytes, 128);
   const uint64_t b_desc = tc05::smem_desc(b_addr, 512, 128);
 #pragma unroll 1
-  for (int w = 0; w < kWindows; ++w) {
+  for (int w = w0; w < kWindows; w += kIssuers) {
     const uint32_t d = d_tmem + ((w & 1) ? 96u + 16u * (uint32_t)(w - 1) : 16u * (uint32_t)w);
 #pragma unroll 1
     for (int dyi = 0; dyi < 17; ++dyi) {
@@ -328,11 +331,15 @@ __device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uin
   }
 }
 
-/* Phase Z, warp 0: for each tile, wait until it is staged and its
- * accumulator buffer has been read out, then issue its MMAs (lane 0) and
- * commit them to mma_done. The whole warp runs the loop so that it reaches
- * the block-wide barriers after the phase converged. */
-__device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int* status) {
+/* Phase Z, warps 0 .. kIssuers-1: for each tile, wait until it is staged and
+ * its accumulator buffer has been read out, then issue the MMAs of windows
+ * w = issuer, issuer + kIssuers, ... (lane 0) and commit them to this
+ * issuer's mma_done barrier: the issuers share the tile's MMA stream (a
+ * single issuing thread, not the tensor pipe, limits the MMA rate here).
+ * Each whole warp runs the loop so that it reaches the block-wide barriers
+ * after the phase converged. */
+__device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int* status,
+                                              int issuer) {
   const int lane = threadIdx.x & 31;
   int j = 0;
   for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
@@ -348,28 +355,30 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
       tc05::fence_after_sync();
       if (ok) {
         issue_tile(tc05::smem_addr(T.smem + (b ? kOffA1 : kOffA0)),
-                   tc05::smem_addr(T.smem + kOffB), T.tmem + (uint32_t)b * kDCols);
+                   tc05::smem_addr(T.smem + kOffB), T.tmem + (uint32_t)b * kDCols, issuer);
       }
-      tc05::mma_commit(&T.mma_done[b]);
+      tc05::mma_commit(&T.mma_done[b * kIssuers + issuer]);
     }
     T.issues[b]++;
     __syncwarp();
   }
 }
 
-/* Phase Z, warps 1..31: stage tile j, then finish tile j - 1: warps 4..11
+/* Phase Z, warps 2..31: stage tile j, then finish tile j - 1: warps 4..11
  * wait for its MMAs and move the accumulators (even + odd windows) to the
  * row-major hand-over tile, and all workers write r_new = r_old - alpha w
  * and z = s K y / sigma + s^2 r_new with coalesced accesses. */
 __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
                                                int* status) {
-  const int tid = threadIdx.x - 32;
+  const int tid = threadIdx.x - 32 * kIssuers;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool reader = warp >= 4 && warp < 4 + kReaders;
   float* zt = reinterpret_cast<float*>(T.smem + kOffZ);
   auto finish = [&](int tile, int bb) {
     if (reader) {
-      const bool ok = tc05::mbar_wait(&T.mma_done[bb], T.done_uses[bb] & 1u, kWaitNs);
+      bool ok = true;
+      for (int i = 0; i < kIssuers; ++i)
+        ok = tc05::mbar_wait(&T.mma_done[bb * kIssuers + i], T.done_uses[bb] & 1u, kWaitNs) && ok;
       T.done_uses[bb]++;
       if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
       tc05::fence_after_sync();
@@ -487,7 +496,7 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     A.sigma = (float)(1.0 / sqrt(rr / n));
     A.zscale = zscale_k / A.sigma;
     ZSums sums = {0.0f, 0.0f, 0.0f};
-    if (threadIdx.x < 32) z_issuer_warp(A, T, P.status);
+    if (threadIdx.x < 32 * kIssuers) z_issuer_warp(A, T, P.status, threadIdx.x >> 5);
     else z_worker_warps(A, T, sums, P.status);
     const float t_rr = block_sum(sums.rr, s_red);
     const float t_rz = block_sum(sums.rz, s_red);
@@ -535,8 +544,8 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   T.smem = smem;
   T.a_full = reinterpret_cast<uint64_t*>(smem + kOffBar);
   T.mma_done = T.a_full + 2;
-  T.d_free = T.a_full + 4;
-  T.drain = T.a_full + 6;
+  T.d_free = T.mma_done + 2 * kIssuers;
+  T.drain = T.d_free + 2;
   for (int b = 0; b < 2; ++b) T.a_uses[b] = T.d_uses[b] = T.issues[b] = T.done_uses[b] = 0;
   uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kOffTmem);
   if (threadIdx.x < 32) {
@@ -546,10 +555,10 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   if (threadIdx.x == 0) {
     for (int b = 0; b < 2; ++b) {
       tc05::mbar_init(&T.a_full[b], 1);
-      tc05::mbar_init(&T.mma_done[b], 1);
+      for (int i = 0; i < kIssuers; ++i) tc05::mbar_init(&T.mma_done[b * kIssuers + i], 1);
       tc05::mbar_init(&T.d_free[b], kReaders);
     }
-    tc05::mbar_init(T.drain, 1);
+    tc05::mbar_init(T.drain, kIssuers);
     tc05::mbar_fence_init();
   }
   for (int i = threadIdx.x; i < kBBytes / 16; i += kThreads)
@@ -564,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
 
   /* Teardown: every MMA this block issued has completed (a commit tracks all
    * of the issuing thread's earlier MMAs), then the tensor memory is freed. */
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32 * kIssuers && (threadIdx.x & 31) == 0) {
     tc05::mma_commit(T.drain);
     if (!tc05::mbar_wait(T.drain, 0, kWaitNs)) atomicCAS(P.status, 0, TL_ERR_TIMEOUT);
   }
