@@ -362,10 +362,20 @@ void run_cg_init(Chunk* chunk, Settings* settings, double rx, double ry,
                     rx, ry, &prm, chunk->p, chunk->r, chunk->u, chunk->u0, chunk->w, chunk->kx,
                     chunk->ky, chunk->density, chunk->energy, &rep),
            "solve");
+    /* algorithmic bytes per cell and inner step of the method's kernel */
+    const double bytes_per_cell = prm.method == TL_METHOD_CG64 ? 104.0
+                                  : prm.method == TL_METHOD_MIXED_CG ? 48.0
+                                  : prm.method == TL_METHOD_MIXED_JACOBI ? 56.0 : 52.0;
+    const double cells = (double)(chunk->x - 2 * settings->halo_depth) *
+                         (double)(chunk->y - 2 * settings->halo_depth);
+    const double gbs = rep.inner_kernel_ms > 0.0f
+                           ? bytes_per_cell * cells * (double)rep.inner_steps /
+                                 ((double)rep.inner_kernel_ms * 1e-3) / 1e9
+                           : 0.0;
     printf("TL_SOLVE method=%d outer=%d inner=%d fallback_events=%d fallback_steps=%d "
-           "rel_residual=%.6e device_ms=%.3f\n",
+           "rel_residual=%.6e device_ms=%.3f inner_gbs=%.1f\n",
            prm.method, rep.outer_steps, rep.inner_steps, rep.fallback_events,
-           rep.fallback_steps, rep.final_rel_residual, rep.device_ms);
+           rep.fallback_steps, rep.final_rel_residual, rep.device_ms, gbs);
     /* One synthetic step with pw = 1, rrn = 0: the driver's loop ends at once. */
     *rro += 1.0;
     ext->ra_rro0 = 1.0;

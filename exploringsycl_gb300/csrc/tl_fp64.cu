@@ -25,12 +25,27 @@
 #include <string>
 
 #include "tl_internal.cuh"
+#include "tl_dmul.cuh"
 
 namespace {
 
 constexpr int kMapThreads = 256;
 constexpr int kRedThreads = 256;
 constexpr int kPersistThreads = 1024;
+/* Which multiplications of the exact persistent CG run on the integer pipes
+ * (tl_dmul.cuh; the products are the same IEEE-rounded values): 0 none, 1 the
+ * stencil's, 2 all. */
+#ifndef TL_INT_DMUL
+#define TL_INT_DMUL 2
+#endif
+constexpr int kIntMul = TL_INT_DMUL;
+
+/* Exact-contract products: on the integer pipes at the given level. */
+template <int kLevel>
+__device__ __forceinline__ double xmul(double a, double b) {
+  if constexpr (kIntMul >= kLevel) return tl_dmul(a, b);
+  return a * b;
+}
 
 /* ------------------------------------------------------------ helpers */
 
@@ -724,7 +739,8 @@ __device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, 
     if (in0) {
       const double s0 =
           kFused ? smvp_fused(dg.x, pc.x, kxp.y, pc.y, kxp.x, pl, kyu.x, pu.x, kyp.x, pd.x)
-                 : dg.x * pc.x - (kxp.y * pc.y + kxp.x * pl) - (kyu.x * pu.x + kyp.x * pd.x);
+                 : xmul<1>(dg.x, pc.x) - (xmul<1>(kxp.y, pc.y) + xmul<1>(kxp.x, pl)) -
+                       (xmul<1>(kyu.x, pu.x) + xmul<1>(kyp.x, pd.x));
       P.w[i0] = s0;
       w0 = s0;
       a0 = pc.x;
@@ -732,7 +748,8 @@ __device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, 
     if (in1) {
       const double s1 =
           kFused ? smvp_fused(dg.y, pc.y, kx2, pr, kxp.y, pc.x, kyu.y, pu.y, kyp.y, pd.y)
-                 : dg.y * pc.y - (kx2 * pr + kxp.y * pc.x) - (kyu.y * pu.y + kyp.y * pd.y);
+                 : xmul<1>(dg.y, pc.y) - (xmul<1>(kx2, pr) + xmul<1>(kxp.y, pc.x)) -
+                       (xmul<1>(kyu.y, pu.y) + xmul<1>(kyp.y, pd.y));
       P.w[i0 + 1] = s1;
       w1 = s1;
       a1 = pc.y;
@@ -753,9 +770,11 @@ __device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, 
               kFused ? smvp_fused(P.diag[i], pc, kx[i + 1], __ldcg(P.p + i + 1), kx[i],
                                   __ldcg(P.p + i - 1), ky[i + x], __ldcg(P.p + i + x), ky[i],
                                   __ldcg(P.p + i - x))
-                     : P.diag[i] * pc -
-                           (kx[i + 1] * __ldcg(P.p + i + 1) + kx[i] * __ldcg(P.p + i - 1)) -
-                           (ky[i + x] * __ldcg(P.p + i + x) + ky[i] * __ldcg(P.p + i - x));
+                     : xmul<1>(P.diag[i], pc) -
+                           (xmul<1>(kx[i + 1], __ldcg(P.p + i + 1)) +
+                            xmul<1>(kx[i], __ldcg(P.p + i - 1))) -
+                           (xmul<1>(ky[i + x], __ldcg(P.p + i + x)) +
+                            xmul<1>(ky[i], __ldcg(P.p + i - x)));
           P.w[i] = s;
           wv[h] = s;
           av[h] = pc;
@@ -765,7 +784,7 @@ __device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, 
     w0 = wv[0]; w1 = wv[1]; a0 = av[0]; a1 = av[1];
   }
   if (kFused) return __fma_rn(w0, a0, w1 * a1);
-  return w0 * a0 + w1 * a1;
+  return xmul<2>(w0, a0) + xmul<2>(w1, a1);
 }
 
 /* u += alpha p, r -= alpha w for the two cells of a lane (fused: one
@@ -776,10 +795,10 @@ __device__ __forceinline__ double ur_pair(const CgPersistParams& P, unsigned i0,
                                           double alpha) {
   const int x = P.x, y = P.y, hd = P.hd;
   auto upd_u = [alpha](double u, double p) {
-    return kFused ? __fma_rn(alpha, p, u) : u + alpha * p;
+    return kFused ? __fma_rn(alpha, p, u) : u + xmul<2>(alpha, p);
   };
   auto upd_r = [alpha](double r, double w) {
-    return kFused ? __fma_rn(-alpha, w, r) : r - alpha * w;
+    return kFused ? __fma_rn(-alpha, w, r) : r - xmul<2>(alpha, w);
   };
   double r0 = 0.0, r1 = 0.0;
   if constexpr (kVec) {
@@ -829,7 +848,7 @@ __device__ __forceinline__ double ur_pair(const CgPersistParams& P, unsigned i0,
     r1 = rv[1];
   }
   if (kFused) return __fma_rn(r0, r0, r1 * r1);
-  return r0 * r0 + r1 * r1;
+  return xmul<2>(r0, r0) + xmul<2>(r1, r1);
 }
 
 /* One CG step loop of TeaLeaf/drivers/cg_driver.c:18-25 with the kernels of
@@ -923,7 +942,7 @@ cg_persistent_kernel(CgPersistParams P) {
         const int kk = (int)(i - (unsigned)jj * (unsigned)x);
         if (!interior(kk, jj, x, y, hd)) continue;
         const double pv = kFused ? __fma_rn(beta, __ldcg(P.p + i), __ldcg(P.r + i))
-                                 : beta * __ldcg(P.p + i) + __ldcg(P.r + i);
+                                 : xmul<2>(beta, __ldcg(P.p + i)) + __ldcg(P.r + i);
         P.p[i] = pv;
         if (kk == hd) P.p[i - 1] = pv;
         if (kk == x - hd - 1) P.p[i + 1] = pv;

@@ -394,9 +394,17 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
   *rep = tl_solve_report{};
   const unsigned len = (unsigned)x * (unsigned)y;
   float ms_total = 0.0f;
-  cudaEvent_t t0, t1;
-  TL_CUDA(cudaEventCreate(&t0));
-  TL_CUDA(cudaEventCreate(&t1));
+  /* the whole solve's events, released on every return path */
+  struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~EventPair() {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+    }
+  } ev;
+  TL_CUDA(cudaEventCreate(&ev.a));
+  TL_CUDA(cudaEventCreate(&ev.b));
+  cudaEvent_t t0 = ev.a, t1 = ev.b;
   TL_CUDA(cudaEventRecord(t0, ctx->stream));
 
   /* Set-up as the reference's cg_init_driver: u = energy*density, kx, ky,
@@ -598,8 +606,6 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
   TL_CUDA(cudaEventRecord(t1, ctx->stream));
   TL_CUDA(cudaEventSynchronize(t1));
   TL_CUDA(cudaEventElapsedTime(&ms_total, t0, t1));
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
   rep->device_ms = ms_total;
   ctx->last_solve.kernel_ms = ms_total;
   ctx->last_solve.steps = rep->inner_steps + rep->fallback_steps;

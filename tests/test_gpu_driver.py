@@ -108,3 +108,17 @@ def test_fused_fp64_contract_under_the_driver(tmp_path, backend_built):
     for se, sf in zip(exact.summaries, fused.summaries):
         for a, b in zip(se, sf):
             assert abs(a - b) <= 1e-10 * abs(a)
+
+
+def test_truncated_weights_file_is_refused(tmp_path, backend_built):
+    """gb300_solver mixed-learned with a weights file one value short: the
+    backend stops the run with an error instead of solving with garbage."""
+    import numpy as np
+    from exploringsycl_gb300.learned import DEFAULT_RAW_WEIGHTS
+    bad = tmp_path / "short.f32"
+    np.fromfile(DEFAULT_RAW_WEIGHTS, dtype="<f4")[:-1].tofile(bad)
+    d = dk.two_state(64, end_step=1)
+    d.extra = ["gb300_solver mixed-learned", f"gb300_weights {bad}"]
+    run = run_driver(DRIVER_EXE, d, tmp_path / "run")
+    assert run.returncode != 0
+    assert "FP32 weights" in run.stdout
