@@ -65,14 +65,17 @@ INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
 # z, p_old, kx, ky, e and writes p_new, w, e (32 B); phase Z reads r, w, s and
 # writes r, z (20 B).
 LEARNED_BYTES = 52
-# FP64 instructions per cell of one CG step: exact contract (stencil 9 with the
+# FP64 operations per cell of one CG step: exact contract (stencil 9 with the
 # precomputed diagonal, dot products 2 x 1.6, u/r update 4, p update 2) and fused
-# multiply-add contract (stencil 5, dot products 2 x 1.6, u/r 2, p 1).
+# multiply-add contract (stencil 5, dot products 2 x 1.6, u/r 2, p 1). Of these,
+# the multiplications without a fused add (10 exact, 2 fused) run on the
+# integer pipes (tl_dmul.cuh); the rest on the FP64 pipe.
 FP64_OPS_PER_CELL_STEP = {"exact": 19, "fused": 11}
+FP64_PIPE_OPS_PER_CELL_STEP = {"exact": 9, "fused": 9}
 # dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
 # each persistent kernel, from one ncu capture (profiles/*.txt).
 NCU_BYTES_PER_CELL_STEP = {
-    ("cg_persistent_kernel", "exact"): 115.4,  # profiles/cg_persistent_fp64_exact_4096.txt
+    ("cg_persistent_kernel", "exact"): 116.9,  # profiles/cg_persistent_fp64_exact_4096.txt
     ("cg_persistent_kernel", "fused"): 120.1,  # profiles/cg_persistent_fp64_fused_4096.txt
     ("inner_cg_kernel", None): 51.3,           # profiles/inner_cg_mixed_jacobi_4096.txt
     ("lpcg_kernel", None): 51.3,               # profiles/lpcg_learned_4096.txt
@@ -431,9 +434,12 @@ def run_ours(args, rank: int, world: int, dist) -> None:
             "peak_source": peaks["source"], "traffic": traffic, "bytes_per_cell_step": bpc,
             "kernel_ms_per_step_avg": k_ms, "kernel_steps_per_timestep": k_steps}
     if kernel == "cg_persistent_kernel":
-        gops = FP64_OPS_PER_CELL_STEP[args.fp64] * cells * k_steps / (k_ms * 1e-3) / 1e9
-        roof.update({"fp64_contract": args.fp64, "fp64_gops": gops,
-                     "fp64_peak_gops": FP64_PEAK_GOPS, "fp64_frac": gops / FP64_PEAK_GOPS})
+        rate = cells * k_steps / (k_ms * 1e-3) / 1e9
+        pipe = FP64_PIPE_OPS_PER_CELL_STEP[args.fp64] * rate
+        roof.update({"fp64_contract": args.fp64,
+                     "fp64_gops": FP64_OPS_PER_CELL_STEP[args.fp64] * rate,
+                     "fp64_pipe_gops": pipe, "fp64_peak_gops": FP64_PEAK_GOPS,
+                     "fp64_pipe_frac": pipe / FP64_PEAK_GOPS})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,

@@ -32,11 +32,12 @@ namespace {
 constexpr int kMapThreads = 256;
 constexpr int kRedThreads = 256;
 constexpr int kPersistThreads = 1024;
-/* Which multiplications of the exact persistent CG run on the integer pipes
+/* Which multiplications of the persistent CG run on the integer pipes
  * (tl_dmul.cuh; the products are the same IEEE-rounded values): 0 none, 1 the
- * stencil's, 2 all. */
+ * exact contract's stencil, 2 all of the exact contract's, 3 also the plain
+ * products of the fused contract. */
 #ifndef TL_INT_DMUL
-#define TL_INT_DMUL 2
+#define TL_INT_DMUL 3
 #endif
 constexpr int kIntMul = TL_INT_DMUL;
 
@@ -693,7 +694,7 @@ constexpr int kWarpsPerTile = TL_GROUP / 8;  /* 8 warps x 8 groups = one tile */
 __device__ __forceinline__ double smvp_fused(double dg, double a, double kr, double ar,
                                              double kl, double al, double ku, double au,
                                              double kd, double ad) {
-  double t = dg * a;
+  double t = xmul<3>(dg, a);
   t = __fma_rn(-kr, ar, t);
   t = __fma_rn(-kl, al, t);
   t = __fma_rn(-ku, au, t);
@@ -783,7 +784,7 @@ __device__ __forceinline__ double w_pair(const CgPersistParams& P, unsigned i0, 
     }
     w0 = wv[0]; w1 = wv[1]; a0 = av[0]; a1 = av[1];
   }
-  if (kFused) return __fma_rn(w0, a0, w1 * a1);
+  if (kFused) return __fma_rn(w0, a0, xmul<3>(w1, a1));
   return xmul<2>(w0, a0) + xmul<2>(w1, a1);
 }
 
@@ -847,7 +848,7 @@ __device__ __forceinline__ double ur_pair(const CgPersistParams& P, unsigned i0,
     r0 = rv[0];
     r1 = rv[1];
   }
-  if (kFused) return __fma_rn(r0, r0, r1 * r1);
+  if (kFused) return __fma_rn(r0, r0, xmul<3>(r1, r1));
   return xmul<2>(r0, r0) + xmul<2>(r1, r1);
 }
 
