@@ -58,33 +58,51 @@ TL_HD double tl_bitsd(uint64_t u) {
 #endif
 }
 
-/* The integer-pipe product; `hw` is the hardware product, used only on the
- * slow path (the caller passes a * b computed without contraction). */
+/* (hi:lo) << s, high word (0 <= s < 32): the funnel shift of the GPU. */
+TL_HD uint32_t tl_shf_l(uint32_t lo, uint32_t hi, uint32_t s) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, s);
+#else
+  return (uint32_t)(((((uint64_t)hi << 32) | lo) << s) >> 32);
+#endif
+}
+
+/* The integer-pipe product of a and b. Operands or results outside the
+ * fast path take the hardware multiplication of the same operands. */
 TL_HD double tl_dmul_int_or(double a, double b, double hw_product_fallback_a,
                             double hw_product_fallback_b) {
   const uint64_t ua = tl_dbits(a), ub = tl_dbits(b);
   const uint32_t ha = (uint32_t)(ua >> 32), hb = (uint32_t)(ub >> 32);
   const uint32_t a0 = (uint32_t)ua, b0 = (uint32_t)ub;
   const uint32_t ea = (ha >> 20) & 0x7FFu, eb = (hb >> 20) & 0x7FFu;
-  const int e = (int)ea + (int)eb - 1023;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 1 || e > 2045) {
+  const uint32_t e = ea + eb - 1023u;  /* biased exponent before normalisation */
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e - 1u >= 2045u) {
     return hw_product_fallback_a * hw_product_fallback_b;
   }
   const uint32_t a1 = (ha & 0xFFFFFu) | 0x100000u;
   const uint32_t b1 = (hb & 0xFFFFFu) | 0x100000u;
+  /* P = w 2^64 + vlo 2^32 + tlo */
   const uint64_t t = (uint64_t)a0 * b0;
-  const uint64_t v = (uint64_t)a0 * b1 + (uint64_t)a1 * b0 + (t >> 32);
+  uint64_t v = (uint64_t)a0 * b1 + (t >> 32);
+  v += (uint64_t)a1 * b0;
   const uint64_t w = (uint64_t)a1 * b1 + (v >> 32);
+  const uint32_t wh = (uint32_t)(w >> 32), wl = (uint32_t)w;
   const uint32_t vlo = (uint32_t)v, tlo = (uint32_t)t;
-  const uint32_t n = (uint32_t)(w >> 41) & 1u;
-  /* m = floor(P / 2^(52+n)) */
-  uint64_t m = (w << (12u - n)) | (uint64_t)(vlo >> (20u + n));
-  const uint32_t round = (vlo >> (19u + n)) & 1u;
-  const uint32_t sticky = ((vlo & ((1u << (19u + n)) - 1u)) | tlo) != 0u;
-  m += (uint64_t)(round & (sticky | (uint32_t)(m & 1u)));
-  const uint64_t sign = (uint64_t)((ha ^ hb) & 0x80000000u) << 32;
-  const uint64_t exp_field = (uint64_t)(e + (int)n - 1) << 52;
-  return tl_bitsd(sign | (exp_field + m));
+  /* n = 1 if P >= 2^105; the significand is P >> (52 + n) = (w:vlo) >> (20 + n),
+   * i.e. the two words of (wh:wl:vlo) << s taken above vlo, s = 12 - n */
+  const uint32_t n = (wh >> 9) & 1u;
+  const uint32_t sh = 12u - n;
+  const uint32_t mh = tl_shf_l(wl, wh, sh);
+  const uint32_t ml = tl_shf_l(vlo, wl, sh);
+  const uint32_t below = vlo << sh;                 /* the bits under the significand */
+  const uint32_t round = below >> 31;
+  const uint32_t sticky = ((below << 1) | tlo) != 0u;
+  const uint32_t inc = round & (sticky | (ml & 1u));
+  /* add the rounding increment and the exponent field (E - 1) << 20 to the
+   * significand's high word (its hidden bit adds the last 1) */
+  const uint64_t lo_sum = (uint64_t)ml + inc;
+  const uint32_t hi = mh + (uint32_t)(lo_sum >> 32) + ((e + n - 1u) << 20);
+  return tl_bitsd(((uint64_t)(hi | ((ha ^ hb) & 0x80000000u)) << 32) | (uint32_t)lo_sum);
 }
 
 /* a * b, correctly rounded, on the integer pipes where possible. */
