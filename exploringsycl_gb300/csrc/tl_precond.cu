@@ -23,7 +23,7 @@
  * K(dy, .) is a product with a banded Toeplitz matrix. A 16-column input
  * window reaches 32 output columns, so one MMA of M = 128 tile rows, N = 32,
  * K = 16 (FP16 inputs, FP32 accumulation in tensor memory, lane = tile row)
- * per window and dy: 85 per 128 x 64 tile, issued by two threads. The A
+ * per window and dy: 85 per 128 x 64 tile, issued by one thread. The A
  * operand is the staged y = sigma S r in the canonical K-major layout
  * (tl_tc05.cuh): chunks of 8 staged columns, each 144 rows x 16 bytes, so a
  * window is two consecutive chunks and the row offset dy a shift of the
@@ -41,8 +41,8 @@
  *   P: (all warps) p_new = z + beta p_old at the cell and its four
  *      neighbours, w = A p_new, p.w partial sums, and the previous step's
  *      e += alpha p_old;
- *   Z: warps 0 and 1 issue each tile's MMAs (even and odd windows) and
- *      commit them to mbarriers; warps 2..31 stage the next tile (r_new = r_old - alpha w and its
+ *   Z: warp 0 issues each tile's MMAs and commits them to an mbarrier;
+ *      warps 1..31 stage the next tile (r_new = r_old - alpha w and its
  *      8-cell halo as y, FP16) into one of two shared buffers and finish the
  *      previous tile: eight of them move its accumulators from tensor memory
  *      into a row-major shared tile, and all of them write r_new and
@@ -70,8 +70,8 @@
 namespace {
 
 constexpr int kThreads = 1024;          /* 32 warps, one block per SM */
-constexpr int kIssuers = 2;             /* phase Z: warps 0, 1 issue the MMAs */
-constexpr int kWorkers = kThreads - 32 * kIssuers;  /* warps 2..31 stage and finish tiles */
+constexpr int kIssuers = 1;             /* phase Z: warp 0 issues the MMAs */
+constexpr int kWorkers = kThreads - 32 * kIssuers;  /* warps 1..31 stage and finish tiles */
 constexpr int kChunk = 4 * kThreads;    /* phase P: cells per block iteration */
 constexpr int kHalo = 8;
 constexpr int kTH = 128;                /* tile rows = MMA M = tensor-memory lanes */
@@ -310,23 +310,37 @@ __device__ __forceinline__ void stage_a(const ZArgs& A, int y0, int x0, unsigned
   }
 }
 
-/* The 85 MMAs of one tile (one thread): input window w (staged columns
- * 16 w .. 16 w + 15, K-major chunks 2 w and 2 w + 1) at row offset
- * dy = dyi - 8 reaches the 32 output columns 16 w - 16 .. 16 w + 15; even
- * and odd windows accumulate into separate column ranges of the buffer, so
- * every window's first MMA (dyi = 0) initialises its own columns. */
-__device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uint32_t d_tmem,
-                                           int w0) {
+/* The MMAs of one tile that issuer kW0 owns (one thread): input window w
+ * (staged columns 16 w .. 16 w + 15, K-major chunks 2 w and 2 w + 1) at row
+ * offset dy = dyi - 8 reaches the 32 output columns 16 w - 16 .. 16 w + 15;
+ * even and odd windows accumulate into separate column ranges of the buffer,
+ * so every window's first MMA (dyi = 0) initialises its own columns. The
+ * loop runs over dy outside and the windows inside: consecutive MMAs then
+ * accumulate into different columns and need not wait for one another. */
+template <int kW0>
+__device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uint32_t d_tmem) {
   const uint64_t a_desc = tc05::smem_desc(a_addr, kChunkBytes, 128);
   const uint64_t b_desc = tc05::smem_desc(b_addr, 512, 128);
 #pragma unroll 1
-  for (int w = w0; w < kWindows; w += kIssuers) {
-    const uint32_t d = d_tmem + ((w & 1) ? 96u + 16u * (uint32_t)(w - 1) : 16u * (uint32_t)w);
-#pragma unroll 1
-    for (int dyi = 0; dyi < 17; ++dyi) {
+  for (int dyi = 0; dyi < 17; ++dyi) {
+    const uint32_t boff = (uint32_t)(dyi * 1024) >> 4;
+#pragma unroll
+    for (int w = kW0; w < kWindows; w += kIssuers) {
+      const uint32_t d = d_tmem + ((w & 1) ? 96u + 16u * (uint32_t)(w - 1) : 16u * (uint32_t)w);
       const uint32_t aoff = (uint32_t)(2 * w * kChunkBytes + dyi * 16) >> 4;
-      const uint32_t boff = (uint32_t)(dyi * 1024) >> 4;
       tc05::mma_f16(d, a_desc + aoff, b_desc + boff, kIdesc, dyi != 0);
+    }
+  }
+}
+
+template <int kW0>
+__device__ __forceinline__ void issue_tile_of(int issuer, uint32_t a_addr, uint32_t b_addr,
+                                              uint32_t d_tmem) {
+  if constexpr (kW0 < kIssuers) {
+    if (issuer == kW0) {
+      issue_tile<kW0>(a_addr, b_addr, d_tmem);
+    } else {
+      issue_tile_of<kW0 + 1>(issuer, a_addr, b_addr, d_tmem);
     }
   }
 }
@@ -334,8 +348,9 @@ __device__ __forceinline__ void issue_tile(uint32_t a_addr, uint32_t b_addr, uin
 /* Phase Z, warps 0 .. kIssuers-1: for each tile, wait until it is staged and
  * its accumulator buffer has been read out, then issue the MMAs of windows
  * w = issuer, issuer + kIssuers, ... (lane 0) and commit them to this
- * issuer's mma_done barrier: the issuers share the tile's MMA stream (a
- * single issuing thread, not the tensor pipe, limits the MMA rate here).
+ * issuer's mma_done barrier. With several issuers the tile's MMA stream is
+ * shared; one issuer with the windows interleaved measured faster than two
+ * or three (0.204 against 0.209 ms per step at 4096^2).
  * Each whole warp runs the loop so that it reaches the block-wide barriers
  * after the phase converged. */
 __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int* status,
@@ -354,8 +369,8 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
     if (lane == 0) {
       tc05::fence_after_sync();
       if (ok) {
-        issue_tile(tc05::smem_addr(T.smem + (b ? kOffA1 : kOffA0)),
-                   tc05::smem_addr(T.smem + kOffB), T.tmem + (uint32_t)b * kDCols, issuer);
+        issue_tile_of<0>(issuer, tc05::smem_addr(T.smem + (b ? kOffA1 : kOffA0)),
+                         tc05::smem_addr(T.smem + kOffB), T.tmem + (uint32_t)b * kDCols);
       }
       tc05::mma_commit(&T.mma_done[b * kIssuers + issuer]);
     }
@@ -364,7 +379,7 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
   }
 }
 
-/* Phase Z, warps 2..31: stage tile j, then finish tile j - 1: warps 4..11
+/* Phase Z, warps kIssuers..31: stage tile j, then finish tile j - 1: warps 4..11
  * wait for its MMAs and move the accumulators (even + odd windows) to the
  * row-major hand-over tile, and all workers write r_new = r_old - alpha w
  * and z = s K y / sigma + s^2 r_new with coalesced accesses. */
