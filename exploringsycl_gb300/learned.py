@@ -6,7 +6,13 @@ tl_net_*); Python only orchestrates.
 * harvest(): seeded random-state problems (the deck distribution of
   deck.random_states) are initialised on the GPU; for each, plain FP64 CG is
   run for a few step counts and the residual after each is kept, packed to
-  FP32, with the problem's FP32 coefficients kx, ky and s = D^-1/2.
+  FP32, with the problem's FP32 coefficients kx, ky and s = D^-1/2. The
+  problems' timestep sets the conduction regime: kx, ky are rx K with
+  rx = dt / dx^2, so a 512^2 problem at dt = 0.004 (4096/512)^2 carries the
+  couplings of a 4096^2 problem at the default dt = 0.004.
+* uniform(): fields of one constant coupling c = rx K each, c log-uniform
+  over the range of a random-state deck, for training on the operator away
+  from material interfaces (the default: see train_cli).
 * train(): Adam on random crops of those residuals, with the loss
   sum ||A M^-1 r - r||^2 / sum ||r||^2 over the batch, on the crop interiors.
 * Weights file: a .npz with the FP32 weight vector, the layout version and a
@@ -158,8 +164,14 @@ class Dataset:
     s: int
 
 
+def like_timestep(size: int, like: int) -> float:
+    """The timestep that gives size^2 problems the rx = dt / dx^2 of like^2
+    problems at the default timestep 0.004."""
+    return 0.004 * (like / size) ** 2
+
+
 def harvest(ctx: Context, n_problems: int, size: int = 512, snapshots=(16, 64, 200),
-            seed0: int = 100000) -> Dataset:
+            seed0: int = 100000, timestep: float = 0.004) -> Dataset:
     """Residual snapshots of plain FP64 CG on seeded random-state problems."""
     from .chunk import GpuChunk
     n = size * size
@@ -171,7 +183,8 @@ def harvest(ctx: Context, n_problems: int, size: int = 512, snapshots=(16, 64, 2
     pw = np.zeros(max(snapshots))
     rr = np.zeros(max(snapshots))
     for prob in range(n_problems):
-        d = dk.random_deck(size, seed=seed0 + prob, end_step=1, max_iters=max(snapshots))
+        d = dk.random_deck(size, seed=seed0 + prob, end_step=1, max_iters=max(snapshots),
+                           initial_timestep=timestep)
         if chunk is None:
             chunk = GpuChunk(d, ctx=ctx)
         else:
@@ -195,6 +208,37 @@ def harvest(ctx: Context, n_problems: int, size: int = 512, snapshots=(16, 64, 2
         check(ctx.lib.tl_pack_coefficients(ctx.h, x, y, hd, f["kx"], f["ky"], ds.kx + off,
                                            ds.ky + off, ds.s + off), "pack coefficients")
     ctx.synchronize()
+    return ds
+
+
+def coupling_range(like: int, density_range=(0.05, 200.0)) -> tuple[float, float]:
+    """The couplings kx = rx (1/d_left + 1/d_right) / 2 of random-state decks
+    (density coefficient) at like^2 cells and dt = 0.004."""
+    rx = 0.004 / (10.0 / like) ** 2
+    return rx / density_range[1], rx / density_range[0]
+
+
+def uniform(ctx: Context, n_problems: int, size: int = 256,
+            c_range: tuple[float, float] = coupling_range(4096), seed: int = 0) -> Dataset:
+    """Constant-coefficient problems: problem p has the coupling c_p
+    (log-uniform in c_range) on every face, s = (1 + 4 c_p)^-1/2, and white
+    noise as its residual. Away from material interfaces the scaled operator
+    S A S of every deck looks like one of these, and a translation-invariant
+    stencil can only be fitted to that part of it: on harvested crops the
+    cells within the stencil's reach of an interface dominate the loss and
+    pull the fit away from what shortens the CG iteration."""
+    rng = np.random.default_rng(seed)
+    n = size * size
+    c = np.exp(rng.uniform(np.log(c_range[0]), np.log(c_range[1]), n_problems))
+    kx = np.repeat(c, n).astype(np.float32)
+    s = np.repeat(1.0 / np.sqrt(1.0 + 4.0 * c), n).astype(np.float32)
+    ds = Dataset(size, n_problems, (0,), ctx.alloc_f32(n * n_problems),
+                 ctx.alloc_f32(n * n_problems), ctx.alloc_f32(n * n_problems),
+                 ctx.alloc_f32(n * n_problems))
+    ctx.upload_f32(ds.r, rng.standard_normal(n * n_problems).astype(np.float32))
+    ctx.upload_f32(ds.kx, kx)
+    ctx.upload_f32(ds.ky, kx)
+    ctx.upload_f32(ds.s, s)
     return ds
 
 
@@ -264,14 +308,15 @@ def evaluate_loss(net: Net, ds: Dataset, batch: int = 32, crop: int = 128, margi
     return tot / rounds
 
 
-def compare_methods(weights: np.ndarray, size: int, seeds, rel_tol: float = 1e-10) -> dict:
+def compare_methods(weights: np.ndarray, size: int, seeds, rel_tol: float = 1e-10,
+                    timestep: float = 0.004) -> dict:
     """Inner steps and device time of the mixed solves (plain, Jacobi,
     learned) on fresh random-state problems of the given seeds."""
     from .chunk import GpuChunk
     out = {m: {"inner_steps": 0, "device_ms": 0.0, "fallbacks": 0}
            for m in ("mixed", "mixed-jacobi", "mixed-learned")}
     for seed in seeds:
-        d = dk.random_deck(size, seed=seed, end_step=1)
+        d = dk.random_deck(size, seed=seed, end_step=1, initial_timestep=timestep)
         for method in out:
             g = GpuChunk(d)
             net = Net(g.ctx, weights) if method == "mixed-learned" else None
@@ -292,14 +337,25 @@ def compare_methods(weights: np.ndarray, size: int, seeds, rel_tol: float = 1e-1
 def train_cli(argv=None) -> None:
     """python -m exploringsycl_gb300.learned --out FILE [--problems N] ...
 
-    Harvests residual snapshots from N seeded 512^2 problems, trains the
-    network from Jacobi-equivalent weights and writes the weights file."""
+    Trains the network from Jacobi-equivalent weights on white-noise
+    residuals and writes the weights file and its raw FP32 twin (.f32). The
+    coefficient crops come from constant-coefficient fields with the
+    couplings of like^2 random-state decks (--data uniform, the default;
+    --like 4096 is the size the preconditioner runs at) or from N seeded
+    512^2 random-state problems harvested in that regime (--data harvest).
+    The evaluation solves fresh random-state problems either way."""
     import argparse
     import time
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    ap.add_argument("--data", choices=["uniform", "harvest"], default="uniform")
     ap.add_argument("--problems", type=int, default=2000)
+    ap.add_argument("--uniform-problems", type=int, default=64)
+    ap.add_argument("--uniform-size", type=int, default=256)
     ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--like", type=int, default=4096,
+                    help="harvest with the timestep that gives the problems the rx = dt/dx^2 "
+                         "of like^2 problems at dt = 0.004")
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--crop", type=int, default=128)
@@ -314,8 +370,14 @@ def train_cli(argv=None) -> None:
     args = ap.parse_args(argv)
     ctx = Context(0)
     t0 = time.time()
-    ds = harvest(ctx, args.problems, size=args.size, seed0=args.seed0,
-                 snapshots=tuple(int(v) for v in args.snapshots.split(",")))
+    dt = like_timestep(args.size, args.like)
+    c_range = coupling_range(args.like)
+    if args.data == "uniform":
+        ds = uniform(ctx, args.uniform_problems, size=args.uniform_size, c_range=c_range,
+                     seed=args.seed0)
+    else:
+        ds = harvest(ctx, args.problems, size=args.size, seed0=args.seed0,
+                     snapshots=tuple(int(v) for v in args.snapshots.split(",")), timestep=dt)
     t1 = time.time()
     net = Net(ctx, identity_weights(noise=1e-3, seed=7))
     before = evaluate_loss(net, ds, crop=args.crop)
@@ -323,7 +385,9 @@ def train_cli(argv=None) -> None:
                  noise_fraction=args.noise_fraction)
     after = evaluate_loss(net, ds, crop=args.crop)
     t2 = time.time()
-    meta = {"problems": args.problems, "size": args.size, "snapshots": list(ds.snapshots),
+    meta = {"data": args.data, "like": args.like, "coupling_range": list(c_range),
+            "problems": ds.n_problems, "size": ds.size, "timestep": dt,
+            "snapshots": list(ds.snapshots),
             "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
             "seed0": args.seed0, "noise_fraction": args.noise_fraction, "loss_jacobi": before, "loss_trained": after,
             "harvest_s": t1 - t0, "train_s": t2 - t1, "history": hist[::max(1, len(hist) // 20)]}
@@ -333,7 +397,12 @@ def train_cli(argv=None) -> None:
                     "results": compare_methods(w, args.eval_size, seeds)}
     meta["eval_small"] = {"size": args.eval_size_small, "seeds": seeds,
                           "results": compare_methods(w, args.eval_size_small, seeds)}
+    dt_small = like_timestep(args.eval_size_small, args.like)
+    meta["eval_like"] = {"size": args.eval_size_small, "timestep": dt_small, "seeds": seeds,
+                         "results": compare_methods(w, args.eval_size_small, seeds,
+                                                    timestep=dt_small)}
     save_weights(args.out, w, meta)
+    export_raw(w, Path(args.out).with_suffix(".f32"))
     print(json.dumps({k: v for k, v in meta.items() if k != "history"}))
     net.close()
     ctx.close()

@@ -167,6 +167,30 @@ def test_trained_network_beats_jacobi_on_unseen_problems(backend_built):
     assert steps["mixed-learned"] < steps["mixed-jacobi"] < steps["mixed"], steps
 
 
+def test_trained_network_in_the_workload_regime(backend_built):
+    """At the couplings of the 4096^2 workload (a 256^2 random-state deck at
+    the timestep that gives it the same rx = dt / dx^2) the committed stencil
+    needs less than half of the Jacobi-preconditioned inner steps."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, like_timestep, load_weights
+    w, _ = load_weights(DEFAULT_WEIGHTS)
+    d = dk.random_deck(256, seed=11, end_step=1, initial_timestep=like_timestep(256, 4096))
+    steps = {}
+    for method in ("mixed-jacobi", "mixed-learned"):
+        g = GpuChunk(d)
+        net = Net(g.ctx, w) if method == "mixed-learned" else None
+        try:
+            rep = g.solve_timestep(method, rel_tol=1e-10, learned=net)
+            assert rep["final_rel_residual"] <= 1e-10, (method, rep)
+            assert rep["fallback_events"] == 0, (method, rep)
+            steps[method] = rep["inner_steps"]
+        finally:
+            if net:
+                net.close()
+            g.close()
+    assert steps["mixed-learned"] < 0.5 * steps["mixed-jacobi"], steps
+
+
 def test_collapsed_stencil_matches_oracle(gpu):
     """K = C^T C as a 17x17 stencil, composed on the GPU from the FP32 master
     weights, against the float64 oracle; the FP16 scale puts max |K| in [0.5, 1)."""
@@ -210,7 +234,10 @@ def test_stencil_application_matches_oracle(gpu, H, W):
 def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
     """The same timestep solved with the fused collapsed-stencil FPCG and with
     the network applied layer by layer: both reach the FP64 target without a
-    fall-back, with inner step counts within 5 % of each other."""
+    fall-back, with inner step counts within 10 % of each other and the
+    collapsed form no slower. The two operators differ only within 8 cells of
+    the edge (the stencil acts once on the zero-extended field, the network
+    truncates every layer), 12 % of the cells of this 256^2 field."""
     from exploringsycl_gb300.chunk import GpuChunk
     from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
     w, _ = load_weights(DEFAULT_WEIGHTS)
@@ -228,7 +255,8 @@ def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
             net.close()
             g.close()
     a, b = steps["mixed-learned"], steps["mixed-learned-layers"]
-    assert abs(a - b) <= 0.05 * b, steps
+    assert abs(a - b) <= 0.10 * b, steps
+    assert a <= 1.02 * b, steps
 
 
 @pytest.mark.parametrize("nx,ny", [(132, 100), (68, 260), (8, 40), (260, 3)])

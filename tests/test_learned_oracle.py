@@ -86,6 +86,34 @@ def test_collapsed_operator_is_symmetric_positive_definite():
     assert ev.min() >= 0.99 * (s ** 2).min()
 
 
+def _constant_coupling_fit(K: np.ndarray, n: int = 128) -> tuple[float, float]:
+    """Mean squared deviation from 1 of the symbol (1 + k(t)) a(t) of
+    S (I + K) S A on a constant coupling c >> 1, where S A S has the symbol
+    a(t) = 1 - (cos tx + cos ty) / 2, and the minimum of k(t)."""
+    t = np.linspace(-np.pi, np.pi, n, endpoint=False) + np.pi / n
+    ty, tx = np.meshgrid(t, t, indexing="ij")
+    a = 1.0 - 0.5 * (np.cos(tx) + np.cos(ty))
+    k = np.zeros_like(a)
+    for dy in range(-8, 9):
+        for dx in range(-8, 9):
+            k += K[dy + 8, dx + 8] * np.cos(dy * ty + dx * tx)
+    return float(np.mean(((1.0 + k) * a - 1.0) ** 2)), float(k.min())
+
+
+def test_committed_stencil_fits_the_constant_coefficient_operator():
+    """Away from material interfaces M^-1 A is similar to (1 + k) a in the
+    symbol picture above; the committed weights bring it close to 1 (mean
+    squared deviation <= 0.15, against ~2 for the Jacobi-equivalent start),
+    with k >= 0 (K positive semi-definite)."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, identity_weights, load_weights
+    w = load_weights(DEFAULT_WEIGHTS)[0].astype(np.float64)
+    fit, kmin = _constant_coupling_fit(nn.collapse(w)[1])
+    start, _ = _constant_coupling_fit(nn.collapse(identity_weights().astype(np.float64))[1])
+    assert fit <= 0.15, fit
+    assert start >= 1.5, start
+    assert kmin >= -1e-9, kmin
+
+
 def test_raw_weights_file_matches_the_npz():
     """The raw FP32 file the run_* backend reads holds the committed weights."""
     from exploringsycl_gb300.learned import DEFAULT_RAW_WEIGHTS, DEFAULT_WEIGHTS, load_weights
