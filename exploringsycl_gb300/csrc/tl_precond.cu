@@ -382,7 +382,9 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
 /* Phase Z, warps kIssuers..31: stage tile j, then finish tile j - 1: warps 4..11
  * wait for its MMAs and move the accumulators (even + odd windows) to the
  * row-major hand-over tile, and all workers write r_new = r_old - alpha w
- * and z = s K y / sigma + s^2 r_new with coalesced accesses. */
+ * and z = s K y / sigma + s^2 r_new with coalesced accesses. The hand-over
+ * tile is single-buffered: a worker barrier separates the last reads of one
+ * tile's rows from the readers' writes of the next. */
 __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
                                                int* status) {
   const int tid = threadIdx.x - 32 * kIssuers;
@@ -395,7 +397,11 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
       for (int i = 0; i < kIssuers; ++i)
         ok = tc05::mbar_wait(&T.mma_done[bb * kIssuers + i], T.done_uses[bb] & 1u, kWaitNs) && ok;
       T.done_uses[bb]++;
+      /* The lanes leave their polling loops at different times; tcgen05.ld
+       * is warp-collective (.sync.aligned) and needs the warp converged. */
+      ok = __all_sync(0xffffffffu, ok);
       if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
+      __syncwarp();
       tc05::fence_after_sync();
       const int sp = warp & 3, half = (warp - 4) >> 2;
       const uint32_t base = T.tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)bb * kDCols +
@@ -404,8 +410,7 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         float ev[16], od[16];
-        tc05::tmem_ld16(base + 16 + 16 * q, ev);       /* even windows: 16 + c */
-        tc05::tmem_ld16(base + 96 + 16 * q, od);       /* odd windows: 96 + c */
+        tc05::tmem_ld16x2(base + 16 + 16 * q, base + 96 + 16 * q, ev, od);
 #pragma unroll
         for (int i = 0; i < 16; ++i) zr[16 * q + i] = ev[i] + od[i];
       }
@@ -453,7 +458,13 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
     prev = tile;
     prev_b = b;
   }
-  if (prev >= 0) finish(prev, prev_b);
+  /* The last tile: its readers overwrite the hand-over tile, so every worker
+   * must have finished reading the previous tile's rows first (inside the
+   * loop the barrier after staging does this). */
+  if (prev >= 0) {
+    named_sync(kBarWorkers, kWorkers);
+    finish(prev, prev_b);
+  }
 }
 
 /* ----------------------------------------------------- persistent FPCG */
@@ -595,6 +606,7 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   tc05::fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) {
+    __syncwarp();
     tc05::fence_after_sync();
     tc05::tmem_dealloc(T.tmem, kTmemCols);
   }
@@ -731,8 +743,8 @@ __global__ void __launch_bounds__(kUThreads) stencil_apply_tc05_kernel(
     const int sp = warp & 3, ch = warp >> 2;
     const int row = 32 * sp + lane, gy = y0 + row;
     float acc[32];
-    tc05::tmem_ld16(tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch, acc);
-    tc05::tmem_ld16(tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch + 16, acc + 16);
+    tc05::tmem_ld16x2(tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch,
+                      tmem + ((uint32_t)(32 * sp) << 16) + 32 * ch + 16, acc, acc + 16);
     if (gy < H) {
 #pragma unroll
       for (int q = 0; q < 8; ++q) {

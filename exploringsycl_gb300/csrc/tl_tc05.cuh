@@ -129,21 +129,34 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity,
   }
 }
 
-/* 32 lanes x 16 columns of 32-bit values: thread t of the warp receives lane
- * (lane field of taddr) + t, columns col .. col + 15. The warp may only
- * address the 32 lanes of its own sub-partition (warp id % 4). */
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
-  uint32_t r[16];
+/* Two loads of 32 lanes x 16 columns of 32-bit values: thread t of the warp
+ * receives lane (lane field of the address) + t, columns col .. col + 15 of
+ * each address. The warp may only address the 32 lanes of its own
+ * sub-partition (warp id % 4). tcgen05.ld is asynchronous: its destination
+ * registers hold the values only after tcgen05.wait::ld, so the loads and the
+ * wait are one asm statement; as two statements the compiler would see no
+ * dependence of the destinations on the wait and could use them before it. */
+__device__ __forceinline__ void tmem_ld16x2(uint32_t taddr_a, uint32_t taddr_b, float va[16],
+                                            float vb[16]) {
+  uint32_t a[16], b[16];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%32];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%33];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3]), "=r"(a[4]), "=r"(a[5]), "=r"(a[6]),
+        "=r"(a[7]), "=r"(a[8]), "=r"(a[9]), "=r"(a[10]), "=r"(a[11]), "=r"(a[12]),
+        "=r"(a[13]), "=r"(a[14]), "=r"(a[15]), "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3]),
+        "=r"(b[4]), "=r"(b[5]), "=r"(b[6]), "=r"(b[7]), "=r"(b[8]), "=r"(b[9]), "=r"(b[10]),
+        "=r"(b[11]), "=r"(b[12]), "=r"(b[13]), "=r"(b[14]), "=r"(b[15])
+      : "r"(taddr_a), "r"(taddr_b)
+      : "memory");
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 16; ++i) {
+    va[i] = __uint_as_float(a[i]);
+    vb[i] = __uint_as_float(b[i]);
+  }
 }
 
 }  // namespace tc05

@@ -259,6 +259,31 @@ def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
     assert a <= 1.02 * b, steps
 
 
+def test_learned_solve_is_deterministic(backend_built):
+    """The same timestep solved twice gives bit-identical fields and inner
+    step counts: at 2048^2 every block of the persistent kernel runs several
+    tiles through the double-buffered tcgen05 pipeline per step, so a race in
+    its hand-over (staged tiles, accumulators, mbarrier phases) would show as
+    a difference."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, like_timestep, load_weights
+    w, _ = load_weights(DEFAULT_WEIGHTS)
+    d = dk.random_deck(2048, seed=3, end_step=1, initial_timestep=like_timestep(2048, 4096))
+    runs = []
+    for _ in range(2):
+        g = GpuChunk(d)
+        net = Net(g.ctx, w)
+        try:
+            rep = g.solve_timestep("mixed-learned", rel_tol=1e-10, learned=net)
+            assert rep["final_rel_residual"] <= 1e-10, rep
+            runs.append((rep["inner_steps"], g.read("u").copy()))
+        finally:
+            net.close()
+            g.close()
+    assert runs[0][0] == runs[1][0], (runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
 @pytest.mark.parametrize("nx,ny", [(132, 100), (68, 260), (8, 40), (260, 3)])
 def test_collapsed_fpcg_on_ragged_fields(nx, ny, backend_built):
     """The persistent tcgen05 solve on interiors that leave ragged 128 x 64
