@@ -34,20 +34,22 @@
  * even and odd windows accumulate into separate tensor-memory columns, and
  * the epilogue adds the two.
  *
- * Flexible PCG (Polak-Ribiere beta = z_new.(r_new - r_old) / z_old.r_old,
- * r_new - r_old = -alpha w), on the packed interior [H][W] with zero-flux
- * edges, one cooperative persistent kernel of one 1024-thread block per SM,
- * two phases and two grid barriers per step:
+ * PCG (beta = z_new.r_new / z_old.r_old: M^-1 is a fixed linear SPD operator,
+ * and the Polak-Ribiere form of flexible PCG measured the same step counts),
+ * on the packed interior [H][W] with zero-flux edges, one cooperative
+ * persistent kernel of one 1024-thread block per SM, two phases and two grid
+ * barriers per step:
  *   P: (all warps) p_new = z + beta p_old at the cell and its four
  *      neighbours, w = A p_new, p.w partial sums, and the previous step's
  *      e += alpha p_old;
  *   Z: warp 0 issues each tile's MMAs and commits them to an mbarrier;
- *      warps 1..31 stage the next tile (r_new = r_old - alpha w and its
- *      8-cell halo as y, FP16) into one of two shared buffers and finish the
- *      previous tile: eight of them move its accumulators from tensor memory
- *      into a row-major shared tile, and all of them write r_new and
- *      z = S K y / sigma + D^-1 r_new with coalesced stores and sum r.r,
- *      r.z and z.w. Staged tiles and accumulators are double-buffered, so
+ *      warps 1..31 stage the next tile: r_new = r_old - alpha w, written to
+ *      memory for the tile's own cells, and with its 8-cell halo as y (FP16)
+ *      into one of two staging buffers; then they finish the previous tile:
+ *      eight of them move its accumulators from tensor memory into a
+ *      row-major shared tile, and all of them read r_new back (from L2) and
+ *      write z = S K y / sigma + D^-1 r_new with coalesced stores and sum
+ *      r.r and r.z. Staged tiles and accumulators are double-buffered, so
  *      the tensor core works while the block streams memory.
  * The residual is double-buffered because a tile reads its neighbours' old
  * residual while they write the new one. Memory per cell and step: P reads z,
@@ -104,7 +106,9 @@ constexpr int kOffZ = kOffB + kBBytes;
 constexpr int kOffBar = kOffZ + kTH * kZStride * 4;
 constexpr int kOffTmem = kOffBar + (5 + 2 * kIssuers) * 8;
 constexpr int kLpcgSmem = (kOffTmem + 8 + 127) / 128 * 128;
-static_assert(kOffB % 128 == 0 && kOffZ % 16 == 0 && kOffBar % 8 == 0, "alignment");
+static_assert(kOffB % 128 == 0 && kOffZ % 16 == 0 && kOffBar % 8 == 0,
+              "alignment");
+static_assert(kLpcgSmem <= 227 * 1024, "shared memory");
 static_assert(2 * kDCols <= kTmemCols, "tensor memory");
 
 struct LpcgParams {
@@ -243,7 +247,7 @@ __device__ __forceinline__ float phase_p(const LpcgParams& P, const float* __res
 /* ------------------------------------------------------------ phase Z */
 
 struct ZSums {
-  float rr, rz, zw;
+  float rr, rz;
 };
 
 struct ZArgs {
@@ -265,13 +269,17 @@ struct TileState {
   uint64_t* d_free;    /* [2] accumulators of buffer b moved out (8 arrivals) */
   uint64_t* drain;     /* every MMA issued so far completed (teardown) */
   uint32_t tmem;
-  uint32_t a_uses[2], d_uses[2], issues[2];  /* issuer */
-  uint32_t done_uses[2];                     /* readers */
+  /* mbarrier phase parities, bit b for buffer b (a runtime-indexed array
+   * would live in local memory): the next a_full / d_free / mma_done phase
+   * to wait for, and whether buffer b has received MMAs before */
+  uint32_t a_par, d_par, issued;  /* issuer */
+  uint32_t done_par;              /* readers */
 };
 
-/* Stages y = sigma * s * (r - alpha w) for tile rows y0-8 .. y0+135 and
- * columns x0-8 .. x0+71 as FP16 into the A buffer (zero outside the domain;
- * W % 4 == 0, so a group of four columns is entirely inside or outside).
+/* Stages y = sigma * s * r_new, r_new = r_old - alpha w, for tile rows
+ * y0-8 .. y0+135 and columns x0-8 .. x0+71 as FP16 into the A buffer (zero
+ * outside the domain; W % 4 == 0, so a group of four columns is entirely
+ * inside or outside), and writes r_new of the tile's own cells to memory.
  * Each thread issues the loads of two groups before it converts them. */
 __device__ __forceinline__ void stage_a(const ZArgs& A, int y0, int x0, unsigned char* abuf,
                                         int tid, int nthr) {
@@ -297,15 +305,21 @@ __device__ __forceinline__ void stage_a(const ZArgs& A, int y0, int x0, unsigned
       if (q >= kTotal) break;
       const int row = q / kGroups, grp = q - row * kGroups;
       const float a = A.alpha, sg = A.sigma;
-      const __half2 lo = __floats2half2_rn(sg * ss[u].x * (r[u].x - a * ww[u].x),
-                                           sg * ss[u].y * (r[u].y - a * ww[u].y));
-      const __half2 hi = __floats2half2_rn(sg * ss[u].z * (r[u].z - a * ww[u].z),
-                                           sg * ss[u].w * (r[u].w - a * ww[u].w));
+      const float4 rv = make_float4(r[u].x - a * ww[u].x, r[u].y - a * ww[u].y,
+                                    r[u].z - a * ww[u].z, r[u].w - a * ww[u].w);
+      const __half2 lo = __floats2half2_rn(sg * ss[u].x * rv.x, sg * ss[u].y * rv.y);
+      const __half2 hi = __floats2half2_rn(sg * ss[u].z * rv.z, sg * ss[u].w * rv.w);
       uint2 packed;
       packed.x = *reinterpret_cast<const uint32_t*>(&lo);
       packed.y = *reinterpret_cast<const uint32_t*>(&hi);
       *reinterpret_cast<uint2*>(abuf + (grp >> 1) * kChunkBytes + row * 16 + (grp & 1) * 8) =
           packed;
+      const int trow = row - kHalo, tcol = 4 * grp - kHalo;
+      if (trow >= 0 && trow < kTH && tcol >= 0 && tcol < kTW) {
+        const int gy = y0 + trow, gx = x0 + tcol;
+        if (gy < A.H && gx < A.W)
+          *reinterpret_cast<float4*>(A.rnew + (size_t)gy * A.W + gx) = rv;
+      }
     }
   }
 }
@@ -359,10 +373,11 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
   int j = 0;
   for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
     const int b = j & 1;
-    bool ok = tc05::mbar_wait(&T.a_full[b], T.a_uses[b] & 1u, kWaitNs);
-    T.a_uses[b]++;
-    if (ok && T.issues[b] > 0) {
-      ok = tc05::mbar_wait(&T.d_free[b], (T.issues[b] - 1u) & 1u, kWaitNs);
+    bool ok = tc05::mbar_wait(&T.a_full[b], (T.a_par >> b) & 1u, kWaitNs);
+    T.a_par ^= 1u << b;
+    if (ok && ((T.issued >> b) & 1u)) {
+      ok = tc05::mbar_wait(&T.d_free[b], (T.d_par >> b) & 1u, kWaitNs);
+      T.d_par ^= 1u << b;
     }
     if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
     __syncwarp();
@@ -374,7 +389,7 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
       }
       tc05::mma_commit(&T.mma_done[b * kIssuers + issuer]);
     }
-    T.issues[b]++;
+    T.issued |= 1u << b;
     __syncwarp();
   }
 }
@@ -385,66 +400,69 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
  * and z = s K y / sigma + s^2 r_new with coalesced accesses. The hand-over
  * tile is single-buffered: a worker barrier separates the last reads of one
  * tile's rows from the readers' writes of the next. */
-__device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
-                                               int* status) {
+/* Finishes one tile of phase Z (worker warps): warps 4..11 wait for its MMAs
+ * and move the accumulators to the hand-over tile zt, then every worker forms
+ * z for its cells from zt, r_new (written by the staging, read back from L2)
+ * and s. */
+__device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSums& sums,
+                                              int* status, int tile, int bb) {
   const int tid = threadIdx.x - 32 * kIssuers;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool reader = warp >= 4 && warp < 4 + kReaders;
   float* zt = reinterpret_cast<float*>(T.smem + kOffZ);
-  auto finish = [&](int tile, int bb) {
-    if (reader) {
-      bool ok = true;
-      for (int i = 0; i < kIssuers; ++i)
-        ok = tc05::mbar_wait(&T.mma_done[bb * kIssuers + i], T.done_uses[bb] & 1u, kWaitNs) && ok;
-      T.done_uses[bb]++;
-      /* The lanes leave their polling loops at different times; tcgen05.ld
-       * is warp-collective (.sync.aligned) and needs the warp converged. */
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
-      __syncwarp();
-      tc05::fence_after_sync();
-      const int sp = warp & 3, half = (warp - 4) >> 2;
-      const uint32_t base = T.tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)bb * kDCols +
-                            (uint32_t)(32 * half);
-      float* zr = zt + (32 * sp + lane) * kZStride + 32 * half;
+  if (reader) {
+    bool ok = true;
+    for (int i = 0; i < kIssuers; ++i)
+      ok = tc05::mbar_wait(&T.mma_done[bb * kIssuers + i], (T.done_par >> bb) & 1u, kWaitNs) &&
+           ok;
+    T.done_par ^= 1u << bb;
+    /* The lanes leave their polling loops at different times; tcgen05.ld
+     * is warp-collective (.sync.aligned) and needs the warp converged. */
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok && lane == 0) atomicCAS(status, 0, TL_ERR_TIMEOUT);
+    __syncwarp();
+    tc05::fence_after_sync();
+    const int sp = warp & 3, half = (warp - 4) >> 2;
+    const uint32_t base = T.tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)bb * kDCols +
+                          (uint32_t)(32 * half);
+    float* zr = zt + (32 * sp + lane) * kZStride + 32 * half;
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        float ev[16], od[16];
-        tc05::tmem_ld16x2(base + 16 + 16 * q, base + 96 + 16 * q, ev, od);
+    for (int q = 0; q < 2; ++q) {
+      float ev[16], od[16];
+      tc05::tmem_ld16x2(base + 16 + 16 * q, base + 96 + 16 * q, ev, od);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) zr[16 * q + i] = ev[i] + od[i];
-      }
-      tc05::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&T.d_free[bb]);
+      for (int i = 0; i < 16; ++i) zr[16 * q + i] = ev[i] + od[i];
     }
-    named_sync(kBarWorkers, kWorkers);
-    const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
-    const int y0 = ty * kTH, x0 = tx * kTW;
-    constexpr int kQuads = kTH * kTW / 4;
-    for (int q = tid; q < kQuads; q += kWorkers) {
-      const int row = q / (kTW / 4), c4 = 4 * (q % (kTW / 4));
-      const int gy = y0 + row, gx = x0 + c4;
-      if (gy >= A.H || gx >= A.W) continue;
-      const size_t i = (size_t)gy * A.W + gx;
-      float4 rn = ld4(A.rold + i);
-      const float4 ww = ld4(A.w + i);
-      rn.x -= A.alpha * ww.x; rn.y -= A.alpha * ww.y;
-      rn.z -= A.alpha * ww.z; rn.w -= A.alpha * ww.w;
-      const float4 ss = __ldg(reinterpret_cast<const float4*>(A.s + i));
-      const float4 acc = *reinterpret_cast<const float4*>(zt + row * kZStride + c4);
-      float4 zv;
-      zv.x = ss.x * (acc.x * A.zscale) + ss.x * ss.x * rn.x;
-      zv.y = ss.y * (acc.y * A.zscale) + ss.y * ss.y * rn.y;
-      zv.z = ss.z * (acc.z * A.zscale) + ss.z * ss.z * rn.z;
-      zv.w = ss.w * (acc.w * A.zscale) + ss.w * ss.w * rn.w;
-      *reinterpret_cast<float4*>(A.z + i) = zv;
-      *reinterpret_cast<float4*>(A.rnew + i) = rn;
-      sums.rr += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
-      sums.rz += rn.x * zv.x + rn.y * zv.y + rn.z * zv.z + rn.w * zv.w;
-      sums.zw += zv.x * ww.x + zv.y * ww.y + zv.z * ww.z + zv.w * ww.w;
-    }
-  };
+    tc05::fence_before_sync();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&T.d_free[bb]);
+  }
+  named_sync(kBarWorkers, kWorkers);
+  const int ty = tile / A.tiles_x, tx = tile - ty * A.tiles_x;
+  const int y0 = ty * kTH, x0 = tx * kTW;
+  constexpr int kQuads = kTH * kTW / 4;
+  for (int q = tid; q < kQuads; q += kWorkers) {
+    const int row = q / (kTW / 4), c4 = 4 * (q % (kTW / 4));
+    const int gy = y0 + row, gx = x0 + c4;
+    if (gy >= A.H || gx >= A.W) continue;
+    const size_t i = (size_t)gy * A.W + gx;
+    const float4 rn = ld4(A.rnew + i);
+    const float4 ss = __ldg(reinterpret_cast<const float4*>(A.s + i));
+    const float4 acc = *reinterpret_cast<const float4*>(zt + row * kZStride + c4);
+    float4 zv;
+    zv.x = ss.x * (acc.x * A.zscale) + ss.x * ss.x * rn.x;
+    zv.y = ss.y * (acc.y * A.zscale) + ss.y * ss.y * rn.y;
+    zv.z = ss.z * (acc.z * A.zscale) + ss.z * ss.z * rn.z;
+    zv.w = ss.w * (acc.w * A.zscale) + ss.w * ss.w * rn.w;
+    *reinterpret_cast<float4*>(A.z + i) = zv;
+    sums.rr += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
+    sums.rz += rn.x * zv.x + rn.y * zv.y + rn.z * zv.z + rn.w * zv.w;
+  }
+}
+
+__device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
+                                               int* status) {
+  const int tid = threadIdx.x - 32 * kIssuers;
   int prev = -1, prev_b = 0, j = 0;
   for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
     const int tile = A.tiles - 1 - c;
@@ -454,7 +472,7 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
     tc05::fence_proxy_async_smem();
     named_sync(kBarWorkers, kWorkers);
     if (tid == 0) mbar_arrive(&T.a_full[b]);
-    if (prev >= 0) finish(prev, prev_b);
+    if (prev >= 0) z_finish_tile(A, T, sums, status, prev, prev_b);
     prev = tile;
     prev_b = b;
   }
@@ -463,7 +481,7 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
    * loop the barrier after staging does this). */
   if (prev >= 0) {
     named_sync(kBarWorkers, kWorkers);
-    finish(prev, prev_b);
+    z_finish_tile(A, T, sums, status, prev, prev_b);
   }
 }
 
@@ -479,7 +497,6 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
   double* part_pw = P.part;
   double* part_rr = P.part + G;
   double* part_rz = P.part + 2 * G;
-  double* part_zw = P.part + 3 * G;
 
   /* r.r of the incoming residual: its RMS sets the FP16 staging scale. */
   {
@@ -521,22 +538,19 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     A.alpha = (float)alpha;
     A.sigma = (float)(1.0 / sqrt(rr / n));
     A.zscale = zscale_k / A.sigma;
-    ZSums sums = {0.0f, 0.0f, 0.0f};
+    ZSums sums = {0.0f, 0.0f};
     if (threadIdx.x < 32 * kIssuers) z_issuer_warp(A, T, P.status, threadIdx.x >> 5);
     else z_worker_warps(A, T, sums, P.status);
     const float t_rr = block_sum(sums.rr, s_red);
     const float t_rz = block_sum(sums.rz, s_red);
-    const float t_zw = block_sum(sums.zw, s_red);
     if (threadIdx.x == 0) {
       part_rr[blockIdx.x] = (double)t_rr;
       part_rz[blockIdx.x] = (double)t_rz;
-      part_zw[blockIdx.x] = (double)t_zw;
     }
     if (!tl_grid_barrier(P.sync, P.status)) return;
     rr = sum_partials(part_rr, G, s_one);
     const double rz = sum_partials(part_rz, G, s_one);
-    const double zw = sum_partials(part_zw, G, s_one);
-    beta = (k == 0) ? 0.0 : -alpha * zw / rz_old;
+    beta = (k == 0) ? 0.0 : rz / rz_old;
     rz_old = rz;
     par_r ^= 1;
     if (k > 0) par_p ^= 1;
@@ -572,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   T.mma_done = T.a_full + 2;
   T.d_free = T.mma_done + 2 * kIssuers;
   T.drain = T.d_free + 2;
-  for (int b = 0; b < 2; ++b) T.a_uses[b] = T.d_uses[b] = T.issues[b] = T.done_uses[b] = 0;
+  T.a_par = T.d_par = T.issued = T.done_par = 0u;
   uint32_t* s_tmem = reinterpret_cast<uint32_t*>(smem + kOffTmem);
   if (threadIdx.x < 32) {
     tc05::tmem_alloc(s_tmem, kTmemCols);
