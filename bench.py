@@ -6,7 +6,7 @@ cells (20-60 rectangles and discs, density log-uniform in [0.05, 200], energy
 uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
 1/density; each timestep solved until the FP64 true residual satisfies
 ||u0 - A u||_2 <= 1e-10 ||u0||_2, with the learned + mixed-precision solver:
-FP32 inner flexible PCG whose preconditioner is the trained network collapsed
+FP32 inner PCG whose preconditioner is the trained network collapsed
 to one 17x17 stencil (tensor cores), inside FP64 iterative refinement. The
 same timesteps are also solved, under the same stop rule, with plain FP64 CG
 in both arithmetic contracts (exact / fused multiply-add) and with the
@@ -61,7 +61,7 @@ BYTES_PER_CELL_STEP = 104          # calc_w 32 + calc_ur 48 + calc_p 24 (FP64)
 # phase 2 reads p_new, w, e, r and writes e, r (24 B); Jacobi adds inv_diag
 # reads in both phases (8 B).
 INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
-# Learned FPCG step (collapsed stencil, one persistent kernel): phase P reads
+# Learned PCG step (collapsed stencil, one persistent kernel): phase P reads
 # z, p_old, kx, ky, e and writes p_new, w, e (32 B); phase Z reads r, w, s and
 # writes r, z (20 B).
 LEARNED_BYTES = 52
@@ -172,7 +172,7 @@ def config_for(args, steps_per_timestep=None) -> dict:
               "cg64": "plain FP64 CG, persistent kernel",
               "mixed": "FP32 inner CG in FP64 iterative refinement",
               "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement",
-              "mixed-learned": "FP32 inner flexible PCG with the learned preconditioner "
+              "mixed-learned": "FP32 inner PCG with the learned preconditioner "
                                "(network collapsed to a 17x17 stencil on the tensor cores) "
                                "in FP64 iterative refinement",
               }[args.solver]

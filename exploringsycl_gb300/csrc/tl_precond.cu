@@ -1,6 +1,6 @@
 /*
  * tl_precond.cu -- the learned preconditioner collapsed to one stencil, and
- * the persistent flexible-PCG kernel of the mixed-precision solver that
+ * the persistent PCG kernel of the mixed-precision solver that
  * applies it on the tensor cores.
  *
  * Collapse. The network of tl_learned.cu has no bias and no activation, so
@@ -485,7 +485,7 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
   }
 }
 
-/* ----------------------------------------------------- persistent FPCG */
+/* ------------------------------------------------------ persistent PCG */
 
 /* The solve; returns when done or when a wait ran out (status set). */
 __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, float* s_red,
@@ -819,7 +819,7 @@ int tl_internal_apply_collapsed(tl_context* ctx, const void* umma, const float* 
   return TL_OK;
 }
 
-/* Inner flexible PCG with the collapsed learned preconditioner on packed
+/* Inner PCG with the collapsed learned preconditioner on packed
  * FP32 arrays: solves A32 e = r until r.r <= tol^2 r0.r0 or max_iters steps.
  * r is the incoming residual (the kernel leaves the final residual in r or
  * r_alt); e, w, z, pa, pb are scratch of H*W floats, all 16-byte aligned.

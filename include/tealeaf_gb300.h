@@ -237,7 +237,7 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
 #define TL_METHOD_CG64 0          /* exact FP64 CG (the drop-in kernel) */
 #define TL_METHOD_MIXED_CG 1      /* FP32 inner CG inside FP64 iterative refinement */
 #define TL_METHOD_MIXED_JACOBI 2  /* as above, Jacobi-preconditioned inner CG */
-#define TL_METHOD_MIXED_LEARNED 3 /* as above, inner flexible PCG with the learned
+#define TL_METHOD_MIXED_LEARNED 3 /* as above, inner PCG with the learned
                                      preconditioner (params->learned) collapsed to
                                      its 17x17 stencil: one persistent kernel,
                                      tensor-core stencil; interior width % 4 == 0 */

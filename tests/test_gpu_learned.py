@@ -259,12 +259,13 @@ def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
     assert a <= 1.02 * b, steps
 
 
-def test_learned_solve_is_deterministic(backend_built):
+@pytest.mark.parametrize("method", ["mixed-learned", "mixed-jacobi", "mixed"])
+def test_mixed_solves_are_deterministic(method, backend_built):
     """The same timestep solved twice gives bit-identical fields and inner
-    step counts: at 2048^2 every block of the persistent kernel runs several
-    tiles through the double-buffered tcgen05 pipeline per step, so a race in
-    its hand-over (staged tiles, accumulators, mbarrier phases) would show as
-    a difference."""
+    step counts: at 2048^2 every block of the persistent kernels runs several
+    tiles (the learned one through its double-buffered tcgen05 pipeline) per
+    step, so a race in a hand-over (staged tiles, accumulators, mbarrier
+    phases, shared tiles) would show as a difference."""
     from exploringsycl_gb300.chunk import GpuChunk
     from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, like_timestep, load_weights
     w, _ = load_weights(DEFAULT_WEIGHTS)
@@ -272,13 +273,14 @@ def test_learned_solve_is_deterministic(backend_built):
     runs = []
     for _ in range(2):
         g = GpuChunk(d)
-        net = Net(g.ctx, w)
+        net = Net(g.ctx, w) if method == "mixed-learned" else None
         try:
-            rep = g.solve_timestep("mixed-learned", rel_tol=1e-10, learned=net)
+            rep = g.solve_timestep(method, rel_tol=1e-10, learned=net)
             assert rep["final_rel_residual"] <= 1e-10, rep
             runs.append((rep["inner_steps"], g.read("u").copy()))
         finally:
-            net.close()
+            if net:
+                net.close()
             g.close()
     assert runs[0][0] == runs[1][0], (runs[0][0], runs[1][0])
     assert np.array_equal(runs[0][1], runs[1][1])
