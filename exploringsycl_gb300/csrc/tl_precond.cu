@@ -364,7 +364,7 @@ __device__ __forceinline__ void issue_tile_of(int issuer, uint32_t a_addr, uint3
  * w = issuer, issuer + kIssuers, ... (lane 0) and commit them to this
  * issuer's mma_done barrier. With several issuers the tile's MMA stream is
  * shared; one issuer with the windows interleaved measured faster than two
- * or three (0.204 against 0.209 ms per step at 4096^2).
+ * or three (by ~2 % of the step time at 4096^2).
  * Each whole warp runs the loop so that it reaches the block-wide barriers
  * after the phase converged. */
 __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int* status,
