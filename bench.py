@@ -495,7 +495,8 @@ def main() -> None:
                     default="mixed-learned")
     ap.add_argument("--fp64", choices=["exact", "fused"], default="exact",
                     help="arithmetic contract of the persistent FP64 CG (plain, cg64, fall-back)")
-    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--inner-tol", type=float, default=0.0,
+                    help="inner FP32 solve reduction (0: the method's default)")
     ap.add_argument("--max-inner", type=int, default=20000,
                     help="inner steps per refinement step (smaller only for profiling captures)")
     ap.add_argument("--max-outer", type=int, default=12)

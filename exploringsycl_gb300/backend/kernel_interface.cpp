@@ -35,7 +35,7 @@
  * network's weights from `gb300_weights <file>` or TL_WEIGHTS: raw
  * little-endian FP32, tl_net_num_params() values), run_cg_init solves the timestep with
  * tl_solve to a relative FP64 true residual (`gb300_rel_tol`, default
- * 1e-10; `gb300_inner_tol`, default 1e-5) and then reports rro = pw = 1,
+ * 1e-10; `gb300_inner_tol`, default the method's own) and then reports rro = pw = 1,
  * rrn = 0, so that the driver's CG loop ends after one pass and prints
  * "CG: 0 iterations"; the backend prints the true counts and the true
  * residual on a TL_SOLVE line. The reference driver ignores the gb300_* keys
@@ -124,7 +124,7 @@ static void load_network(ChunkExtension* ext, const char* path) {
 static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
   ext->replace_method = settings->preconditioner ? TL_METHOD_MIXED_JACOBI : -1;
   ext->replace_rel_tol = 1e-10;
-  ext->replace_inner_tol = 1e-5;
+  ext->replace_inner_tol = 0.0; /* the method's default */
   ext->fp64_fused = 0;
   char weights[512] = "";
   FILE* f = fopen(settings->tea_in_filename, "r");

@@ -113,7 +113,7 @@ class GpuChunk:
         return steps.value
 
     def solve_timestep(self, method: str = "mixed", rel_tol: float = 1e-10,
-                       inner_tol: float = 1e-5, max_inner: int = 20000, max_outer: int = 12,
+                       inner_tol: float = 0.0, max_inner: int = 20000, max_outer: int = 12,
                        stall_factor: float = 0.5, max_fallback: int = 20000,
                        learned=None) -> dict:
         """One timestep solved to a relative FP64 true residual with one of

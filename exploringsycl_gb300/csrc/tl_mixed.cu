@@ -14,7 +14,9 @@
  *
  * Outer step (FP64): r = u0 - A u; stop if small; r32 = r * s (s scales the
  * residual to unit RMS); solve A32 e = r32 in FP32 to a relative reduction
- * inner_tol; u += e / s. The inner operator A32 uses kx, ky rounded to FP32
+ * inner_tol (0: the method's default, 1e-6 with the learned preconditioner,
+ * whose restarts cost more than its extra inner steps, 1e-5 otherwise);
+ * u += e / s. The inner operator A32 uses kx, ky rounded to FP32
  * and the flux form a + sum k (a - a_nb), in which a neighbour across the
  * domain boundary equals the cell itself (the reflective halo), so boundary
  * fluxes vanish exactly.
@@ -450,6 +452,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
                "tl_solve: unknown method");
     const bool layers = prm->method == TL_METHOD_MIXED_LEARNED_LAYERS;
     const bool learned = layers || prm->method == TL_METHOD_MIXED_LEARNED;
+    const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : (learned ? 1e-6 : 1e-5);
     TL_REQUIRE(!learned || prm->learned, "tl_solve: the learned method needs a network");
     const int H = y - 2 * hd, W = x - 2 * hd;
     TL_REQUIRE(!layers || (H % 4 == 0 && W % 64 == 0),
@@ -515,7 +518,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
       const double scale = sqrt((double)(x - 2 * hd) * (double)(y - 2 * hd)) / rn;
       if (learned) {
         const double need = 0.5 * target / rn;
-        const double tol = std::max(prm->inner_tol, std::min(need, 0.5));
+        const double tol = std::max(inner_tol, std::min(need, 0.5));
         rc = tl_pack_interior(ctx, x, y, hd, r, scale, r32);
         if (rc != TL_OK) return rc;
         int it = 0;
@@ -562,7 +565,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
        * a factor 0.5 of margin), so the last refinement step does not
        * overshoot the target. */
       const double need = 0.5 * target / rn;
-      const double tol = std::max(prm->inner_tol, std::min(need, 0.5));
+      const double tol = std::max(inner_tol, std::min(need, 0.5));
       P.tol2 = tol * tol;
       P.kx = kx32; P.ky = ky32; P.invd = invd;
       P.r = r32; P.e = e32; P.w = w32; P.pa = pa; P.pb = pb;

@@ -249,7 +249,9 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
 typedef struct tl_solve_params {
   int method;           /* TL_METHOD_* */
   double rel_tol;       /* relative FP64 true-residual target */
-  double inner_tol;     /* residual reduction asked of each inner FP32 solve */
+  double inner_tol;     /* residual reduction asked of each inner FP32 solve;
+                           0 selects the method's default (1e-6 for the
+                           learned methods, 1e-5 otherwise) */
   int max_inner;        /* inner CG steps per outer step (CG64: total steps) */
   int max_outer;        /* refinement steps */
   double stall_factor;  /* an outer step must shrink the residual below
