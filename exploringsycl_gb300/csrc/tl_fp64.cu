@@ -73,13 +73,6 @@ struct PlainLoad {
   __device__ __forceinline__ double operator()(unsigned i) const { return p[i]; }
 };
 
-/* Loads that bypass L1: for fields that other blocks of the same
- * persistent kernel rewrite between grid barriers. */
-struct L2Load {
-  const double* p;
-  __device__ __forceinline__ double operator()(unsigned i) const { return __ldcg(p + i); }
-};
-
 /* ---------------------------------------------------------- map kernels */
 
 template <class Op>
