@@ -14,7 +14,7 @@
  *
  * Outer step (FP64): r = u0 - A u; stop if small; r32 = r * s (s scales the
  * residual to unit RMS); solve A32 e = r32 in FP32 to a relative reduction
- * inner_tol (0: the method's default, 1e-6 with the learned preconditioner,
+ * inner_tol (0: the method's default, 3e-6 with the learned preconditioner,
  * whose restarts cost more than its extra inner steps, 1e-5 otherwise);
  * u += e / s. The inner operator A32 uses kx, ky rounded to FP32
  * and the flux form a + sum k (a - a_nb), in which a neighbour across the
@@ -452,7 +452,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
                "tl_solve: unknown method");
     const bool layers = prm->method == TL_METHOD_MIXED_LEARNED_LAYERS;
     const bool learned = layers || prm->method == TL_METHOD_MIXED_LEARNED;
-    const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : (learned ? 1e-6 : 1e-5);
+    const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : (learned ? 3e-6 : 1e-5);
     TL_REQUIRE(!learned || prm->learned, "tl_solve: the learned method needs a network");
     const int H = y - 2 * hd, W = x - 2 * hd;
     TL_REQUIRE(!layers || (H % 4 == 0 && W % 64 == 0),

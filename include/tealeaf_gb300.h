@@ -250,7 +250,7 @@ typedef struct tl_solve_params {
   int method;           /* TL_METHOD_* */
   double rel_tol;       /* relative FP64 true-residual target */
   double inner_tol;     /* residual reduction asked of each inner FP32 solve;
-                           0 selects the method's default (1e-6 for the
+                           0 selects the method's default (3e-6 for the
                            learned methods, 1e-5 otherwise) */
   int max_inner;        /* inner CG steps per outer step (CG64: total steps) */
   int max_outer;        /* refinement steps */
