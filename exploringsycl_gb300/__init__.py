@@ -130,6 +130,7 @@ HANDLE_FIRST = {
     "tl_net_adam_step": [C.c_float],
     "tl_net_stencil": [C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "tl_net_apply_stencil": [_I, _I, _P, _P, _P],
+    "tl_net_pcg": [_I, _I, _P, _P, _P, _P, _P, _D, _I, _PI, _PD],
     "tl_net_gather_crops": [_P, _I, _I, C.POINTER(C.c_int), _I, _I, _I, _P],
     "tl_pack_interior": [_I, _I, _I, _P, _D, _P],
     "tl_pack_coefficients": [_I, _I, _I, _P, _P, _P, _P, _P],

@@ -950,6 +950,23 @@ __global__ void pack_kernel(int x, int y, int hd, const double* __restrict__ src
 }
 
 /* kx, ky and s = (diag)^-1/2 of the packed FP32 operator */
+/* s = D^-1/2 of the packed operator: D = 1 + the couplings of the faces
+ * inside the field. */
+__global__ void packed_scaling_kernel(int H, int W, const float* __restrict__ kx,
+                                      const float* __restrict__ ky, float* __restrict__ s) {
+  const size_t n = (size_t)H * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int xx = (int)(i % W), yy = (int)(i / W);
+    float d = 1.0f;
+    if (xx + 1 < W) d += kx[i + 1];
+    if (xx > 0) d += kx[i];
+    if (yy + 1 < H) d += ky[i + W];
+    if (yy > 0) d += ky[i];
+    s[i] = rsqrtf(d);
+  }
+}
+
 __global__ void pack_coeff_kernel(int x, int y, int hd, const double* __restrict__ kx,
                                   const double* __restrict__ ky, float* __restrict__ pkx,
                                   float* __restrict__ pky, float* __restrict__ ps) {
@@ -1123,6 +1140,30 @@ extern "C" int tl_net_apply_stencil(tl_net* net, int H, int W, const float* r, c
   TL_REQUIRE(net && r && s && z, "tl_net_apply_stencil: null argument");
   return tl_internal_apply_collapsed(net->ctx, net->stencil_umma, net->stencil_kscale, H, W, r,
                                      s, z);
+}
+
+extern "C" int tl_net_pcg(tl_net* net, int H, int W, const float* kx, const float* ky,
+                          const float* b, float* e, float* work, double tol, int max_iters,
+                          int* iters, double* rr) {
+  TL_REQUIRE(net && kx && ky && b && e && work, "tl_net_pcg: null argument");
+  TL_REQUIRE(H > 0 && W > 0 && W % 4 == 0, "tl_net_pcg: needs H > 0 and W % 4 == 0");
+  tl_context* ctx = net->ctx;
+  const size_t n = (size_t)H * W;
+  float* s = work;
+  float* r = work + n;
+  packed_scaling_kernel<<<grid1d(ctx, n), 256, 0, ctx->stream>>>(H, W, kx, ky, s);
+  TL_CHECK_LAUNCH(ctx);
+  TL_CUDA(cudaMemcpyAsync(r, b, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  int it = 0;
+  double rr_final = 0.0;
+  const int rc = tl_internal_fpcg_collapsed(ctx, net->stencil_umma32, net->stencil_kscale, H, W,
+                                            kx, ky, s, r, work + 2 * n, e, work + 3 * n,
+                                            work + 4 * n, work + 5 * n, work + 6 * n, tol,
+                                            max_iters, &it, &rr_final);
+  if (rc != TL_OK) return rc;
+  if (iters) *iters = it;
+  if (rr) *rr = rr_final;
+  return TL_OK;
 }
 
 int tl_internal_net_stencil(tl_net* net, const void** umma, const float** kscale) {

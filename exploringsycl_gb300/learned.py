@@ -147,6 +147,16 @@ class Net:
         check(self.lib.tl_net_apply_stencil(self.h, H, W, r_dev, s_dev, z_dev),
               "tl_net_apply_stencil")
 
+    def pcg(self, H, W, kx_dev, ky_dev, b_dev, e_dev, work_dev, tol: float,
+            max_iters: int) -> tuple[int, float]:
+        """The learned PCG on packed [H][W] fields: A e = b to r.r <= tol^2 b.b
+        or max_iters steps (work: 7 H*W floats). Returns (steps, final r.r)."""
+        it = C.c_int(0)
+        rr = C.c_double(0.0)
+        check(self.lib.tl_net_pcg(self.h, H, W, kx_dev, ky_dev, b_dev, e_dev, work_dev, tol,
+                                  max_iters, C.byref(it), C.byref(rr)), "tl_net_pcg")
+        return it.value, rr.value
+
     def close(self) -> None:
         if self.h:
             self.lib.tl_net_destroy(self.h)

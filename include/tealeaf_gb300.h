@@ -317,6 +317,17 @@ int tl_net_stencil(tl_net* net, float* host_k, float* kscale);
  * accumulation). */
 int tl_net_apply_stencil(tl_net* net, int H, int W, const float* r, const float* s,
                          float* z);
+/* The learned PCG on its own, on packed FP32 [H][W] fields (W % 4 == 0):
+ * solves A e = b, (A v)_i = v_i + sum over the cell's faces inside the field
+ * of k (v_i - v_nb) (kx[j][i] couples cells i-1 and i of row j, ky[j][i] rows
+ * j-1 and j; couplings across the field's edges are ignored: zero flux),
+ * preconditioned by the network's collapsed stencil, M^-1 = D^-1 + S K S
+ * with S = D^-1/2 from the same couplings, by the persistent tensor-core
+ * kernel of the learned solver, until r.r <= tol^2 b.b or max_iters steps.
+ * b, e and the couplings are device arrays of H*W floats; work holds 7 more.
+ * iters and rr (may be NULL) receive the step count and the final r.r. */
+int tl_net_pcg(tl_net* net, int H, int W, const float* kx, const float* ky, const float* b,
+               float* e, float* work, double tol, int max_iters, int* iters, double* rr);
 /* out[b] = crop of data[meta[3b]] at rows meta[3b+1].., columns meta[3b+2]..
  * (data: device [P][HS][WS]; meta: host int triples). */
 int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, int WS,

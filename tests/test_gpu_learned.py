@@ -259,6 +259,79 @@ def test_collapsed_fpcg_follows_the_layer_by_layer_network(backend_built):
     assert a <= 1.02 * b, steps
 
 
+def _pcg_restated(K, kx, ky, b, steps):
+    """PCG (beta = r.z / r_old.z_old) in float64 on A v = v + sum over the
+    faces inside the field of k (v - v_nb), M^-1 = D^-1 + S K S: the
+    algorithm of the persistent learned kernel, step for step."""
+    from oracle import nn_oracle as nn
+
+    def apply_a(v):
+        out = v.copy()
+        f = kx[:, 1:] * (v[:, 1:] - v[:, :-1])
+        out[:, 1:] += f
+        out[:, :-1] -= f
+        g = ky[1:, :] * (v[1:, :] - v[:-1, :])
+        out[1:, :] += g
+        out[:-1, :] -= g
+        return out
+
+    d = np.ones_like(b)
+    d[:, 1:] += kx[:, 1:]
+    d[:, :-1] += kx[:, 1:]
+    d[1:, :] += ky[1:, :]
+    d[:-1, :] += ky[1:, :]
+    s = 1.0 / np.sqrt(d)
+    r = b.copy()
+    e = np.zeros_like(b)
+    z = nn.apply_collapsed(K, r, s)
+    rz = float(np.sum(r * z))
+    p = z.copy()
+    for _ in range(steps):
+        w = apply_a(p)
+        alpha = rz / float(np.sum(p * w))
+        e += alpha * p
+        r -= alpha * w
+        z = nn.apply_collapsed(K, r, s)
+        rz_new = float(np.sum(r * z))
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return e, float(np.sum(r * r))
+
+
+@pytest.mark.parametrize("H,W", [(72, 132), (200, 256)])
+def test_learned_pcg_kernel_follows_the_restated_algorithm(gpu, H, W):
+    """The persistent tensor-core PCG (tl_net_pcg) against a float64
+    restatement with the oracle's collapsed preconditioner, after 1, 2 and 5
+    steps: solution and r.r within the FP16 staging's error. The couplings
+    across the field's edges are random and must be ignored (zero flux)."""
+    from exploringsycl_gb300.learned import DEFAULT_WEIGHTS, Net, load_weights
+    from oracle import nn_oracle as nn
+    w = load_weights(DEFAULT_WEIGHTS)[0]
+    _, K = nn.collapse(w.astype(np.float64))
+    rng = np.random.default_rng(H + W)
+    kx = np.exp(rng.uniform(0.0, np.log(1000.0), (H, W))).astype(np.float32)
+    ky = np.exp(rng.uniform(0.0, np.log(1000.0), (H, W))).astype(np.float32)
+    b = rng.standard_normal((H, W)).astype(np.float32)
+    net = Net(gpu, w)
+    try:
+        d = _upload(gpu, {"kx": kx, "ky": ky, "b": b})
+        e_dev = gpu.alloc_f32(H * W)
+        work = gpu.alloc_f32(7 * H * W)
+        for steps in (1, 2, 5):
+            it, rr = net.pcg(H, W, d["kx"], d["ky"], d["b"], e_dev, work, 1e-30, steps)
+            assert it == steps
+            got = gpu.download_f32(e_dev, H * W).reshape(H, W)
+            want, rr_want = _pcg_restated(K, kx.astype(np.float64), ky.astype(np.float64),
+                                          b.astype(np.float64), steps)
+            assert np.linalg.norm(got - want) <= 3e-2 * np.linalg.norm(want), steps
+            assert abs(rr - rr_want) <= 5e-2 * rr_want, (steps, rr, rr_want)
+        # and the solve reaches its target
+        it, rr = net.pcg(H, W, d["kx"], d["ky"], d["b"], e_dev, work, 1e-5, 5000)
+        assert 0 < it < 5000 and rr <= 1e-10 * float(np.sum(b.astype(np.float64) ** 2))
+    finally:
+        net.close()
+
+
 @pytest.mark.parametrize("method", ["mixed-learned", "mixed-jacobi", "mixed"])
 def test_mixed_solves_are_deterministic(method, backend_built):
     """The same timestep solved twice gives bit-identical fields and inner
