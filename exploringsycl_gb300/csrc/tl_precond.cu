@@ -119,7 +119,7 @@ struct LpcgParams {
   float *e, *w, *z, *p0, *p1;
   const __half* umma;  /* window B operands, 17 x 32 x 16 FP16 */
   const float* kscale;
-  double* part;  /* 4 arrays of gridDim.x partial sums */
+  double* part;  /* 3 arrays of gridDim.x partial sums: p.w, r.r, r.z */
   unsigned* sync;
   int* status;
   int* iters_out;
@@ -260,8 +260,8 @@ struct ZArgs {
   float alpha, sigma, zscale;
 };
 
-/* Per-block tcgen05 state. The counters are kept by the threads that wait on
- * each mbarrier, so that every wait names the parity of the phase it needs. */
+/* Per-block tcgen05 state. The phase parities are kept by the threads that
+ * wait on each mbarrier, so that every wait names the phase it needs. */
 struct TileState {
   unsigned char* smem;
   uint64_t* a_full;    /* [2] staged tile b is in shared memory (1 arrival) */
@@ -394,16 +394,11 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
   }
 }
 
-/* Phase Z, warps kIssuers..31: stage tile j, then finish tile j - 1: warps 4..11
- * wait for its MMAs and move the accumulators (even + odd windows) to the
- * row-major hand-over tile, and all workers write r_new = r_old - alpha w
- * and z = s K y / sigma + s^2 r_new with coalesced accesses. The hand-over
- * tile is single-buffered: a worker barrier separates the last reads of one
- * tile's rows from the readers' writes of the next. */
 /* Finishes one tile of phase Z (worker warps): warps 4..11 wait for its MMAs
- * and move the accumulators to the hand-over tile zt, then every worker forms
- * z for its cells from zt, r_new (written by the staging, read back from L2)
- * and s. */
+ * and move the accumulators (even + odd windows) to the row-major hand-over
+ * tile zt, then every worker forms z = s K y / sigma + s^2 r_new for its cells
+ * from zt, r_new (written by the staging, read back from L2) and s, with
+ * coalesced accesses, and sums r.r and r.z. */
 __device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSums& sums,
                                               int* status, int tile, int bb) {
   const int tid = threadIdx.x - 32 * kIssuers;
@@ -460,6 +455,10 @@ __device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSum
   }
 }
 
+/* Phase Z, warps kIssuers..31: stage tile j (writing r_new = r_old - alpha w
+ * for its own cells), then finish tile j - 1. The hand-over tile is
+ * single-buffered: a worker barrier separates the last reads of one tile's
+ * rows from the readers' writes of the next. */
 __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
                                                int* status) {
   const int tid = threadIdx.x - 32 * kIssuers;
