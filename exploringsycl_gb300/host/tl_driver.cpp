@@ -11,7 +11,7 @@
  * absent; oracle/Makefile's `ref` target links the reference's own driver
  * against the CPU oracle to show that both drivers print identical results.
  *
- * Deliberate differences, each also listed in the design doc:
+ * Deliberate differences from the reference driver:
  *  - the tridiagonal eigenvalue problem of the Chebyshev/PPCG solvers is
  *    solved by Sturm-sequence bisection (own code) instead of the reference's
  *    QL iteration (drivers/eigenvalue_driver.c:71-122), so Chebyshev and
