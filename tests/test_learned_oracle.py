@@ -120,3 +120,39 @@ def test_raw_weights_file_matches_the_npz():
     w, _ = load_weights(DEFAULT_WEIGHTS)
     raw = np.fromfile(DEFAULT_RAW_WEIGHTS, dtype="<f4")
     assert raw.shape == w.shape and np.array_equal(raw, w)
+
+
+def _oracle_couplings(n, seed, timestep):
+    """Interior face couplings kx (x faces inside the field) of a random-state
+    deck, as the oracle's cg_init_k computes them."""
+    import ctypes as C
+
+    from exploringsycl_gb300 import deck as dk
+    from oracle import oracle as O
+    d = dk.random_deck(n, seed=seed, end_step=1, initial_timestep=timestep)
+    ch = O.OracleChunk(d)
+    rx, ry = ch.rx_ry()
+    ch.halos(["energy", "density"], 2)
+    ch.L.orc_cg_init_u(ch.x, ch.y, ch.coefficient, ch.p("p"), ch.p("r"), ch.p("u"), ch.p("w"),
+                       ch.p("density"), ch.p("energy"))
+    ch.L.orc_cg_init_k(ch.x, ch.y, ch.hd, ch.p("w"), ch.p("kx"), ch.p("ky"), C.c_double(rx),
+                       C.c_double(ry))
+    hd = ch.hd
+    kx = ch.f["kx"].reshape(ch.y, ch.x)[hd:ch.y - hd, hd + 1:ch.x - hd]
+    return kx
+
+
+def test_training_couplings_cover_the_workload(oracle_built):
+    """The constant-coefficient training fields take their couplings from
+    coupling_range(like): every interior coupling of a random-state deck at
+    like^2 cells lies in that range, and like_timestep gives a smaller deck
+    the couplings of the larger one (kx = rx K, rx = dt / dx^2)."""
+    from exploringsycl_gb300.learned import coupling_range, like_timestep
+    lo, hi = coupling_range(256)
+    kx = _oracle_couplings(256, 5, 0.004)
+    assert kx.min() >= lo * (1 - 1e-12) and kx.max() <= hi * (1 + 1e-12)
+    assert kx.max() >= 0.2 * hi and kx.min() <= 5.0 * lo  # the deck spans most of it
+    small = _oracle_couplings(64, 5, like_timestep(64, 256))
+    lo64, hi64 = coupling_range(256)
+    assert small.min() >= lo64 * (1 - 1e-12) and small.max() <= hi64 * (1 + 1e-12)
+    assert abs(like_timestep(512, 4096) - 0.256) < 1e-15
