@@ -20,6 +20,8 @@ LIB_PATH = BUILD / "libtealeaf_gb300.so"
 DRIVER_EXE = BUILD / "tealeaf_gb300"
 
 TL_OK = 0
+# Largest grid (x*y cells, halos included): TL_MAX_CELLS of include/tealeaf_gb300.h.
+MAX_CELLS = 536_870_912
 TL_ERRORS = {1: "TL_ERR_CUDA", 2: "TL_ERR_ARG", 3: "TL_ERR_TIMEOUT", 4: "TL_ERR_STATE",
              5: "TL_ERR_NUMERIC"}
 

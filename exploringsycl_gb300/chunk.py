@@ -13,8 +13,8 @@ import math
 
 import numpy as np
 
-from . import (CONDUCTIVITY, METHODS, Context, TLSolveParams, TLSolveReport, TLState,
-               check)
+from . import (CONDUCTIVITY, MAX_CELLS, METHODS, Context, TLError, TLSolveParams,
+               TLSolveReport, TLState, check)
 from .deck import Deck
 
 GEOMETRY = {"rectangle": 0, "circular": 1, "point": 2}
@@ -46,11 +46,14 @@ def parsed_states(deck: Deck) -> list[TLState]:
 class GpuChunk:
     def __init__(self, deck: Deck, ctx: Context | None = None, device: int = 0):
         self.deck = deck
-        self.ctx = ctx or Context(device)
         self.hd = deck.halo_depth or 2
         self.x = deck.x_cells + 2 * self.hd
         self.y = deck.y_cells + 2 * self.hd
         self.n = self.x * self.y
+        if self.n > MAX_CELLS:
+            raise TLError(f"grid of {self.x} x {self.y} cells (halos included) exceeds "
+                          f"TL_MAX_CELLS ({MAX_CELLS} cells)")
+        self.ctx = ctx or Context(device)
         self.dx = (deck.xmax - deck.xmin) / deck.x_cells
         self.dy = (deck.ymax - deck.ymin) / deck.y_cells
         self.coefficient = CONDUCTIVITY if deck.coefficient in (None, "density") else 2

@@ -957,8 +957,15 @@ cg_persistent_kernel(CgPersistParams P) {
 /* ================================================================ ABI */
 
 #define CTX_OK(ctx) TL_REQUIRE((ctx) != nullptr, "null context")
-#define DIMS_OK(x, y, hd) \
-  TL_REQUIRE((x) > 2 * (hd) && (y) > 2 * (hd) && (hd) >= 1, "invalid grid dimensions")
+#define CELLS_OK(x, y)                                                                 \
+  TL_REQUIRE((x) > 0 && (y) > 0 && (size_t)(x) * (size_t)(y) <= (size_t)TL_MAX_CELLS,  \
+             "invalid grid dimensions (at most TL_MAX_CELLS cells)")
+#define DIMS_OK(x, y, hd)                                                              \
+  do {                                                                                 \
+    TL_REQUIRE((x) > 2 * (hd) && (y) > 2 * (hd) && (hd) >= 1, "invalid grid dimensions"); \
+    TL_REQUIRE((size_t)(x) * (size_t)(y) <= (size_t)TL_MAX_CELLS,                      \
+               "grid larger than TL_MAX_CELLS (536,870,912 cells)");                   \
+  } while (0)
 
 extern "C" int tl_set_chunk_data_vertices(tl_context* ctx, int x, int y, int hd,
                                           double* vertex_x, double* vertex_y,
@@ -990,6 +997,7 @@ extern "C" int tl_set_chunk_initial_state(tl_context* ctx, int x, int y,
                                           double default_density, double* energy0,
                                           double* density) {
   CTX_OK(ctx);
+  CELLS_OK(x, y);
   return launch_map(ctx, InitialStateOp{default_energy, default_density, energy0, density},
                     x, y);
 }
@@ -1010,6 +1018,7 @@ extern "C" int tl_set_chunk_state(tl_context* ctx, int x, int y, int hd,
 extern "C" int tl_store_energy(tl_context* ctx, int x, int y, double* energy,
                                const double* energy0) {
   CTX_OK(ctx);
+  CELLS_OK(x, y);
   return launch_map(ctx, CopyAllOp{energy, energy0}, x, y);
 }
 

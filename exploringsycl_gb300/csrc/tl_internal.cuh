@@ -32,6 +32,8 @@
 #define TL_GROUP 64                       /* cells per first-level group */
 #define TL_TILE (TL_GROUP * TL_GROUP)     /* cells per tile (4096) */
 #define TL_MAX_TILES (1 << 17)            /* grids up to 5.4e8 cells */
+static_assert((long long)TL_MAX_TILES * TL_TILE == TL_MAX_CELLS,
+              "the public grid limit is the reduction scratch's");
 /* Shared scratch of a block-wide reduction of up to TL_MAX_TILES partials:
  * the first level (TL_MAX_TILES/64 values), then the smaller levels. */
 #define TL_RED_SCRATCH (TL_MAX_TILES / TL_GROUP + TL_MAX_TILES / TL_TILE + 64)

@@ -1206,6 +1206,9 @@ extern "C" int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, i
 extern "C" int tl_pack_interior(tl_context* ctx, int x, int y, int hd, const double* field,
                                 double scale, float* packed) {
   TL_REQUIRE(ctx && field && packed, "tl_pack_interior: null argument");
+  TL_REQUIRE(x > 2 * hd && y > 2 * hd && hd >= 1 &&
+                 (size_t)x * (size_t)y <= (size_t)TL_MAX_CELLS,
+             "tl_pack_interior: invalid grid dimensions");
   pack_kernel<<<grid1d(ctx, (size_t)x * y), 256, 0, ctx->stream>>>(x, y, hd, field, scale, packed);
   TL_CHECK_LAUNCH(ctx);
   return TL_OK;
@@ -1214,6 +1217,9 @@ extern "C" int tl_pack_interior(tl_context* ctx, int x, int y, int hd, const dou
 extern "C" int tl_pack_coefficients(tl_context* ctx, int x, int y, int hd, const double* kx,
                                     const double* ky, float* pkx, float* pky, float* ps) {
   TL_REQUIRE(ctx && kx && ky && pkx && pky && ps, "tl_pack_coefficients: null argument");
+  TL_REQUIRE(x > 2 * hd && y > 2 * hd && hd >= 1 &&
+                 (size_t)x * (size_t)y <= (size_t)TL_MAX_CELLS,
+             "tl_pack_coefficients: invalid grid dimensions");
   pack_coeff_kernel<<<grid1d(ctx, (size_t)x * y), 256, 0, ctx->stream>>>(x, y, hd, kx, ky, pkx,
                                                                           pky, ps);
   TL_CHECK_LAUNCH(ctx);

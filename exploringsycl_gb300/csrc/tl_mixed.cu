@@ -392,6 +392,8 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
                         const double* density, const double* energy, tl_solve_report* rep) {
   TL_REQUIRE(ctx && prm && rep, "tl_solve: null argument");
   TL_REQUIRE(x > 2 * hd && y > 2 * hd && hd >= 1, "invalid grid dimensions");
+  TL_REQUIRE((size_t)x * (size_t)y <= (size_t)TL_MAX_CELLS,
+             "grid larger than TL_MAX_CELLS (536,870,912 cells)");
   TL_REQUIRE(prm->rel_tol > 0.0, "tl_solve: rel_tol must be positive");
   *rep = tl_solve_report{};
   const unsigned len = (unsigned)x * (unsigned)y;

@@ -14,6 +14,9 @@
  *    index kk + jj*x, x = x_cells + 2*halo_depth, y = y_cells + 2*halo_depth,
  *    interior kk in [halo_depth, x-halo_depth), jj in [halo_depth, y-halo_depth).
  *    Allocate them with tl_field_alloc (256-byte aligned, zero-filled).
+ *    A grid holds at most TL_MAX_CELLS cells, halos included (23,170^2; the
+ *    deterministic reductions keep every partial sum of one level in one
+ *    block's shared memory); calls on larger grids return TL_ERR_ARG.
  *  - Every call is issued on the context's stream. Calls that return a
  *    scalar through a host pointer synchronise that stream before returning;
  *    the others return as soon as the work is queued.
@@ -45,6 +48,9 @@ extern "C" {
 #define TL_ERR_TIMEOUT 3   /* a bounded in-kernel wait gave up */
 #define TL_ERR_STATE 4     /* call out of sequence */
 #define TL_ERR_NUMERIC 5   /* non-finite value or breakdown in a solver */
+
+/* Largest grid, x*y cells including halos (131,072 reduction tiles of 4096). */
+#define TL_MAX_CELLS 536870912
 
 /* Geometry codes of a state (TeaLeaf/settings.h:130-135). */
 #define TL_RECTANGULAR 0

@@ -44,3 +44,20 @@ def test_oracle_exports(oracle_built):
     L = oracle_built.lib()
     for name in oracle_built.SIGNATURES:
         assert hasattr(L, name)
+
+
+def test_grid_limit_matches_the_header_and_is_checked_before_any_allocation():
+    """TL_MAX_CELLS (the deterministic reductions' largest grid, 131,072 tiles
+    of 4096 cells) is one number in the header and the package, and a chunk
+    above it is refused before a context or a field is made."""
+    import re
+
+    import pytest
+
+    from exploringsycl_gb300 import deck as dk
+    from exploringsycl_gb300.chunk import GpuChunk
+    text = (tl.PKG.parent / "include" / "tealeaf_gb300.h").read_text()
+    assert int(re.search(r"#define TL_MAX_CELLS (\d+)", text).group(1)) == tl.MAX_CELLS
+    assert tl.MAX_CELLS == 131072 * 4096
+    with pytest.raises(tl.TLError, match="TL_MAX_CELLS"):
+        GpuChunk(dk.two_state(23168))  # 23172^2 cells with the halos
