@@ -20,6 +20,10 @@ PROBLEMS = """512 512 20 1.034697091898282e+02
 """Expected final temperatures of the five-state deck, by (x_cells, y_cells,
 end_step), as tabulated by the reference (TeaLeaf/tea.problems:1-9)."""
 
+EDGE_RUNS = ("point_state_32x2", "capped_64x2", "strip_1x40x2", "strip_40x1x2")
+"""Golden runs of edge cases: a point state, a CG solve stopped by max_iters,
+interiors one cell wide. On the GPU they have their own test module."""
+
 
 @dataclass
 class Run:

@@ -13,6 +13,7 @@ Usage: python tests/golden/make_golden.py
 from __future__ import annotations
 
 import json
+import math
 import re
 import subprocess
 import sys
@@ -25,6 +26,25 @@ sys.path.insert(0, str(ROOT))
 from exploringsycl_gb300 import deck as dk  # noqa: E402
 from oracle import oracle  # noqa: E402
 from tests.drivers import run_driver  # noqa: E402
+
+
+
+def _point_on_vertex(vertex: float, d: float) -> float:
+    """The deck coordinate that the reference's parser turns into `vertex`:
+    it adds d/100 to a state's xmin/ymin (TeaLeaf/parse_config.c:254-256) and
+    paints a point state only where a vertex equals that sum exactly
+    (c_kernels/sycl/set_chunk_state.cpp:68-73), so a point given at a vertex's
+    own coordinate paints nothing."""
+    v = vertex - d / 100.0
+    for _ in range(64):
+        if v + d / 100.0 == vertex:
+            return v
+        v = math.nextafter(v, math.inf if v + d / 100.0 < vertex else -math.inf)
+    raise ValueError("no deck coordinate reaches the vertex")
+
+
+_BG = dk.five_state(1).states
+_PT = _point_on_vertex(5.0, 10.0 / 32)  # the vertex at x = y = 5 of a 32^2 mesh on [0, 10]^2
 
 DECKS = {
     "five_state_10x10": dk.five_state(10, end_step=10),
@@ -39,6 +59,13 @@ DECKS = {
     "jacobi_40x2": dk.five_state(40, end_step=2, max_iters=400, solver="jacobi"),
     "cheby_64x2": dk.five_state(64, end_step=2, solver="chebyshev", presteps=8),
     "ppcg_64x2": dk.five_state(64, end_step=2, solver="ppcg", presteps=8),
+    # edge cases: a point state (one cell), CG stopped by max_iters before it
+    # converges, and one-cell-wide strips (interior narrower than the halo)
+    "point_state_32x2": dk.Deck(32, 32, _BG[:2] + [dk.State(0.1, 25.0, "point", _PT, _PT, _PT,
+                                                            _PT)], end_step=2),
+    "capped_64x2": dk.five_state(64, end_step=2, max_iters=20),
+    "strip_1x40x2": dk.Deck(1, 40, _BG, end_step=2),
+    "strip_40x1x2": dk.Deck(40, 1, _BG, end_step=2),
 }
 
 FORTRAN_OUT = {1: "tea_bm_1.out", 2: "tea_bm_2.out", 3: "tea_bm_3.out"}

@@ -11,7 +11,7 @@ import pytest
 from exploringsycl_gb300 import DRIVER_EXE
 from exploringsycl_gb300 import deck as dk
 
-from .drivers import run_driver
+from .drivers import EDGE_RUNS, run_driver
 
 pytestmark = pytest.mark.gpu
 
@@ -79,7 +79,8 @@ class _TextDeck:
         Path(path).write_text(self._t)
 
 
-@pytest.mark.parametrize("name", [n for n in GOLDEN["runs"] if not n.startswith(("cheby", "ppcg"))])
+@pytest.mark.parametrize("name", [n for n in GOLDEN["runs"]
+                                  if not n.startswith(("cheby", "ppcg")) and n not in EDGE_RUNS])
 def test_gpu_driver_matches_reference_driver_golden(name, tmp_path, backend_built):
     """The GB300 backend under this project's driver prints exactly what the
     reference's own driver printed with the oracle kernels: CG step counts,
