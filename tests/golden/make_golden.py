@@ -15,7 +15,6 @@ from __future__ import annotations
 import json
 import math
 import re
-import subprocess
 import sys
 import tempfile
 from pathlib import Path

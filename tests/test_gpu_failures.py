@@ -5,9 +5,9 @@ from __future__ import annotations
 
 import ctypes as C
 
-import numpy as np
 import pytest
 
+import exploringsycl_gb300 as tl
 from exploringsycl_gb300 import TLError
 from exploringsycl_gb300 import deck as dk
 
@@ -37,3 +37,26 @@ def test_invalid_arguments_are_refused(backend_built):
         status = C.c_int(0)
         with pytest.raises(TLError):   # budget above one second
             ctx.call("tl_selftest_barrier_timeout", 5000, C.byref(status))
+
+
+def test_grid_dimensions_are_argument_errors(backend_built):
+    """Grids above TL_MAX_CELLS and non-positive sizes are refused with
+    TL_ERR_ARG by the host before anything is launched."""
+    side = 23172  # 23172^2 > TL_MAX_CELLS
+    with tl.Context(0) as ctx:
+        lib = ctx.lib
+        buf = ctx.alloc(16)
+        before = ctx.launches()
+        pw = C.c_double(0.0)
+        assert lib.tl_cg_calc_w(ctx.h, side, side, 2, None, None, None, None,
+                                C.byref(pw)) == 2
+        assert b"TL_MAX_CELLS" in lib.tl_last_error()
+        assert lib.tl_set_chunk_initial_state(ctx.h, -1, 8, 1.0, 1.0, None, None) == 2
+        assert lib.tl_store_energy(ctx.h, 8, 0, None, None) == 2
+        assert lib.tl_pack_interior(ctx.h, side, side, 2, buf, 1.0, buf) == 2
+        prm = tl.TLSolveParams(method=tl.METHOD_MIXED_CG, rel_tol=1e-10)
+        rep = tl.TLSolveReport()
+        assert lib.tl_solve(ctx.h, side, side, 2, 1, 1.0, 1.0, C.byref(prm), *([None] * 9),
+                            C.byref(rep)) == 2
+        assert b"TL_MAX_CELLS" in lib.tl_last_error()
+        assert ctx.launches() == before
