@@ -4,7 +4,8 @@ Runs the reference's own, unchanged TeaLeaf host driver (compiled from the
 reference sources by `make -C oracle ref`, linked with the CPU oracle
 kernels) on a set of decks, and records what it prints: CG step counts,
 per-step error, the full-precision field summaries and the pass/fail check.
-Also records the final field summaries that the reference's Fortran runs
+The 4096^2 deck of TeaLeaf/tea.problems is recorded apart ("full_size"): one
+CPU run of it takes about three minutes. Also records the final field summaries that the reference's Fortran runs
 printed in TeaLeaf/Benchmarks/tea_bm_{1,2,3}.out (line 173 of each).
 
 Needs the reference sources (default /root/reference/TeaLeaf, or TEALEAF_REF).
@@ -67,6 +68,10 @@ DECKS = {
     "strip_40x1x2": dk.Deck(40, 1, _BG, end_step=2),
 }
 
+# The largest deck that the reference tabulates (TeaLeaf/tea.problems:2): kept
+# apart from DECKS because one CPU run of it takes minutes.
+FULL_SIZE = {"five_state_4096x1": dk.five_state(4096, end_step=1)}
+
 FORTRAN_OUT = {1: "tea_bm_1.out", 2: "tea_bm_2.out", 3: "tea_bm_3.out"}
 
 
@@ -84,20 +89,21 @@ def fortran_summaries() -> dict:
 
 def main() -> None:
     oracle.build(with_reference=True)
-    runs = {}
+    runs, full = {}, {}
     with tempfile.TemporaryDirectory() as tmp:
-        for name, d in DECKS.items():
-            r = run_driver(oracle.REF_DRIVER, d, Path(tmp) / name)
-            assert r.returncode == 0, r.stdout[-1000:]
-            runs[name] = {"deck": d.text(), "iterations": r.iterations, "errors": r.errors,
-                          "summaries": [list(s) for s in r.summaries],
-                          "passed": r.passed,
-                          "expected": re.findall(r"^Expected (\S+)", r.stdout, re.M),
-                          "actual": re.findall(r"^Actual\s+(\S+)", r.stdout, re.M)}
+        for table, decks in ((runs, DECKS), (full, FULL_SIZE)):
+            for name, d in decks.items():
+                r = run_driver(oracle.REF_DRIVER, d, Path(tmp) / name, timeout=3600)
+                assert r.returncode == 0, r.stdout[-1000:]
+                table[name] = {"deck": d.text(), "iterations": r.iterations,
+                               "errors": r.errors, "summaries": [list(s) for s in r.summaries],
+                               "passed": r.passed,
+                               "expected": re.findall(r"^Expected (\S+)", r.stdout, re.M),
+                               "actual": re.findall(r"^Actual\s+(\S+)", r.stdout, re.M)}
     out = {"generator": "tests/golden/make_golden.py",
            "driver": "reference TeaLeaf host driver (TeaLeaf/*.c, drivers/*.c, -DNO_MPI) "
                      "linked with oracle/tl_oracle.c",
-           "runs": runs, "fortran_step10": fortran_summaries()}
+           "runs": runs, "full_size": full, "fortran_step10": fortran_summaries()}
     path = Path(__file__).with_name("reference_driver_runs.json")
     path.write_text(json.dumps(out, indent=1))
     print(f"wrote {path}")

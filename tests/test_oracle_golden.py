@@ -60,6 +60,23 @@ def test_tabulated_temperatures_pass(name):
     assert abs(100.0 * act / exp - 100.0) < 0.001
 
 
+def test_full_size_tabulated_deck():
+    """The largest deck the reference tabulates, 4096^2 for one step
+    (TeaLeaf/tea.problems:2): the reference's driver with the oracle kernels
+    reproduces the tabulated temperature to 1e-12 and passes its own 0.001 %
+    check; the domain's volume is exact. That run takes minutes, so its
+    record is checked here and replayed on the GPU bit for bit."""
+    from .drivers import PROBLEMS
+    rec = GOLDEN["full_size"]["five_state_4096x1"]
+    row = next(ln.split() for ln in PROBLEMS.splitlines() if ln.startswith("4096 4096 1 "))
+    assert rec["expected"] == [row[3]]
+    assert rec["passed"] is True and rec["iterations"] == [4996]
+    vol, mass, ie, temp = rec["summaries"][-1]
+    assert vol == 100.0
+    assert math.isclose(temp, float(row[3]), rel_tol=1e-12)
+    assert math.isclose(temp, float(rec["actual"][0]), rel_tol=1e-15)
+
+
 @pytest.mark.parametrize("bm,name", [(1, "five_state_10x10"), (2, "five_state_250x10"),
                                      (3, "five_state_500x10")])
 def test_fortran_reference_summaries(bm, name):

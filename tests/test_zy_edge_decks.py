@@ -1,10 +1,12 @@
 """Edge cases under the TeaLeaf host driver on the GPU, against what the
 reference's own driver printed with the oracle kernels: a point state that
-paints one cell, a CG solve stopped by max_iters before it converges, and
-interiors one cell wide (narrower than the halo). CG step counts, per-step
+paints one cell, a CG solve stopped by max_iters before it converges,
+interiors one cell wide (narrower than the halo), and the largest deck that
+the reference tabulates (4096^2, one step of 4996 CG iterations, whose
+reductions run three levels of partial sums). CG step counts, per-step
 errors and full-precision field summaries must agree bit for bit, with the
-whole timestep solved on the device and replayed (fused) and with one kernel
-per driver call (stepwise).
+whole timestep solved on the device and replayed (fused) and, for the small
+decks, with one kernel per driver call (stepwise).
 
 Collected after the other GPU modules and before the allocation-free entry
 point's, so that a run stopping at the first failure has run those first."""
@@ -42,3 +44,13 @@ def test_edge_decks_match_reference_driver_golden(name, mode, tmp_path, backend_
     assert r.errors == g["errors"]
     assert [list(s) for s in r.summaries] == g["summaries"]
     assert r.passed == g["passed"]
+
+
+def test_full_size_tabulated_deck_matches_reference_driver_bitwise(tmp_path, backend_built):
+    g = GOLDEN["full_size"]["five_state_4096x1"]
+    r = run_driver(DRIVER_EXE, _TextDeck(g["deck"]), tmp_path)
+    assert r.returncode == 0, r.stdout[-1000:]
+    assert r.passed is True
+    assert r.iterations == g["iterations"]
+    assert r.errors == g["errors"]
+    assert [list(s) for s in r.summaries] == g["summaries"]
