@@ -22,7 +22,11 @@
  * bit-identical to the device's (both are the same IEEE divisions of the
  * same recorded values); a mismatch stops the run with an error. The final
  * device state, the scalars and the iteration count are those of the
- * step-wise path, bit for bit.
+ * step-wise path, bit for bit. Should the driver ask for more steps than
+ * the device recorded (the device stopped early: both apply the same stop
+ * rule to the same values), the replay ends after the last recorded step
+ * and the remaining steps run on the step-wise kernels from the device's
+ * final state.
  *
  * Errors. Every failing call ends the run through die() with the backend's
  * message, as the reference's fatal errors do (TeaLeaf/shared.c:98-111).

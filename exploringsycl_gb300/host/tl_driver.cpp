@@ -5,7 +5,7 @@
  *
  * This is a restatement, in this project's own code, of the behaviour of the
  * reference's unchanged C driver (TeaLeaf/main.c, diffuse.c, initialise.c,
- * parse_config.c, settings.c, shared.c, chunk.c, profiler.c, drivers/*.c),
+ * parse_config.c, settings.c, shared.c, chunk.c, profiler.c, drivers/),
  * built without MPI (one rank). The reference driver cannot travel with this
  * repository, so this file plays its part wherever the reference sources are
  * absent; oracle/Makefile's `ref` target links the reference's own driver
