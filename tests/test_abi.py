@@ -61,3 +61,42 @@ def test_grid_limit_matches_the_header_and_is_checked_before_any_allocation():
     assert tl.MAX_CELLS == 131072 * 4096
     with pytest.raises(tl.TLError, match="TL_MAX_CELLS"):
         GpuChunk(dk.two_state(23168))  # 23172^2 cells with the halos
+
+
+def test_bindings_match_the_header_prototypes():
+    """Every ctypes binding passes as many arguments as its C prototype has,
+    each of the same kind (int, size_t, float, double, pointer): a slip
+    between the two would pass garbage without any error."""
+    import re
+
+    text = re.sub(r"/\*.*?\*/", "", (tl.PKG.parent / "include" / "tealeaf_gb300.h").read_text(),
+                  flags=re.S)
+    protos = {}
+    for m in re.finditer(r"^\s*(?:int|const char\*|long long)\s+(tl_\w+)\(([^;]*?)\);", text,
+                         re.M | re.S):
+        body = m.group(2).strip()
+        protos[m.group(1)] = [] if body in ("", "void") else [p.strip() for p in body.split(",")]
+
+    def c_kind(param):
+        param = re.sub(r"\s+", " ", param)
+        if "*" in param:
+            return "pointer"
+        for kind in ("double", "float", "size_t", "int"):
+            if re.match(rf"(const )?{kind}\b", param):
+                return kind
+        return param
+
+    def py_kind(t):
+        if t is C.c_void_p or (isinstance(t, type) and issubclass(t, C._Pointer)):
+            return "pointer"
+        return {C.c_double: "double", C.c_float: "float", C.c_size_t: "size_t",
+                C.c_int: "int"}.get(t, repr(t))
+
+    checked = 0
+    for table, leading in ((tl.SIGNATURES, [C.c_void_p]), (tl.HANDLE_FIRST, [C.c_void_p]),
+                           (tl.CONTEXT_FREE, [])):
+        for name, args in table.items():
+            assert [py_kind(t) for t in leading + list(args)] == \
+                [c_kind(p) for p in protos[name]], name
+            checked += 1
+    assert checked >= 45
