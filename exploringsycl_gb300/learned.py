@@ -264,14 +264,36 @@ def gather(ctx: Context, ds: Dataset, which: str, meta: np.ndarray, crop: int, o
                                       crop, out), "gather")
 
 
+def smooth_probes(noise: np.ndarray, c: np.ndarray, k: float) -> np.ndarray:
+    """White-noise crops [B][H][W] filtered by a_c(theta)^(-k/2) and scaled
+    to unit RMS, where a_c = (1 + 2c (2 - cos theta_x - cos theta_y)) /
+    (1 + 4c) is the symbol of the scaled operator S A S for the constant
+    coupling c[b] of crop b. Under the loss ||A M^-1 r - r||^2 such probes
+    weigh the misfit at frequency theta by a_c^-k: the low frequencies, where
+    CG converges slowly, count more than under white noise (k = 0). The
+    filter is periodic over the crop; the loss leaves out a margin at the
+    crop's edge."""
+    B, H, W = noise.shape
+    ty = 2.0 * np.pi * np.fft.fftfreq(H)[:, None]
+    tx = 2.0 * np.pi * np.fft.fftfreq(W)[None, :]
+    c = np.asarray(c, dtype=np.float64).reshape(B, 1, 1)
+    a = (1.0 + 2.0 * c * (2.0 - np.cos(ty) - np.cos(tx))) / (1.0 + 4.0 * c)
+    r = np.fft.ifft2(np.fft.fft2(noise.astype(np.float64)) * a ** (-0.5 * k)).real
+    r /= np.sqrt(np.mean(r * r, axis=(1, 2), keepdims=True))
+    return r.astype(np.float32)
+
+
 def train(net: Net, ds: Dataset, steps: int = 2000, batch: int = 32, crop: int = 128,
           lr: float = 1e-3, margin: int = 9, seed: int = 0, log_every: int = 100,
-          lr_decay_at: float = 0.7, noise_fraction: float = 0.0) -> list[tuple[int, float]]:
+          lr_decay_at: float = 0.7, noise_fraction: float = 0.0,
+          probe_smoothing: float = 0.0) -> list[tuple[int, float]]:
     """Adam on random crops; returns (step, loss) samples. With
     noise_fraction > 0 that share of the residual crops is replaced by white
     noise on the same coefficient crops, so that the loss also weighs the
     upper part of the spectrum (a least-squares fit of M^-1 A to I over all
-    modes) and not only the smooth modes that dominate CG residuals."""
+    modes) and not only the smooth modes that dominate CG residuals. With
+    probe_smoothing = k > 0 that noise is filtered by smooth_probes with each
+    crop's mean coupling, which weighs the misfit at low frequencies more."""
     ctx = net.ctx
     rng = np.random.default_rng(seed)
     n = batch * crop * crop
@@ -287,7 +309,11 @@ def train(net: Net, ds: Dataset, steps: int = 2000, batch: int = 32, crop: int =
         n_noise = int(round(noise_fraction * batch))
         if n_noise:
             r_host = ctx.download_f32(bufs["r"], n).reshape(batch, crop, crop)
-            r_host[:n_noise] = rng.standard_normal((n_noise, crop, crop)).astype(np.float32)
+            noise = rng.standard_normal((n_noise, crop, crop)).astype(np.float32)
+            if probe_smoothing > 0.0:
+                kx = ctx.download_f32(bufs["kx"], n).reshape(batch, crop, crop)[:n_noise]
+                noise = smooth_probes(noise, kx.mean(axis=(1, 2)), probe_smoothing)
+            r_host[:n_noise] = noise
             ctx.upload_f32(bufs["r"], r_host)
         loss, _ = net.loss_grad(crop, crop, batch, margin, bufs["r"], bufs["s"], bufs["kx"],
                                 bufs["ky"])
@@ -374,6 +400,8 @@ def train_cli(argv=None) -> None:
     ap.add_argument("--snapshots", default="2,8,32",
                     help="CG step counts at which residuals are harvested")
     ap.add_argument("--noise-fraction", type=float, default=1.0)
+    ap.add_argument("--probe-smoothing", type=float, default=0.0,
+                    help="k: filter the noise probes by a^(-k/2) (0: white noise)")
     ap.add_argument("--eval-size", type=int, default=1024)
     ap.add_argument("--eval-size-small", type=int, default=512)
     ap.add_argument("--eval-seeds", default="7,8")
@@ -392,14 +420,15 @@ def train_cli(argv=None) -> None:
     net = Net(ctx, identity_weights(noise=1e-3, seed=7))
     before = evaluate_loss(net, ds, crop=args.crop)
     hist = train(net, ds, steps=args.steps, batch=args.batch, crop=args.crop, lr=args.lr,
-                 noise_fraction=args.noise_fraction)
+                 noise_fraction=args.noise_fraction, probe_smoothing=args.probe_smoothing)
     after = evaluate_loss(net, ds, crop=args.crop)
     t2 = time.time()
     meta = {"data": args.data, "like": args.like, "coupling_range": list(c_range),
             "problems": ds.n_problems, "size": ds.size, "timestep": dt,
             "snapshots": list(ds.snapshots),
             "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
-            "seed0": args.seed0, "noise_fraction": args.noise_fraction, "loss_jacobi": before, "loss_trained": after,
+            "seed0": args.seed0, "noise_fraction": args.noise_fraction,
+            "probe_smoothing": args.probe_smoothing, "loss_jacobi": before, "loss_trained": after,
             "harvest_s": t1 - t0, "train_s": t2 - t1, "history": hist[::max(1, len(hist) // 20)]}
     w = net.get()
     seeds = [int(v) for v in args.eval_seeds.split(",")]

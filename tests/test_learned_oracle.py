@@ -156,3 +156,28 @@ def test_training_couplings_cover_the_workload(oracle_built):
     lo64, hi64 = coupling_range(256)
     assert small.min() >= lo64 * (1 - 1e-12) and small.max() <= hi64 * (1 + 1e-12)
     assert abs(like_timestep(512, 4096) - 0.256) < 1e-15
+
+
+def test_smoothed_probes_follow_the_operator_symbol():
+    """smooth_probes multiplies every Fourier coefficient of the noise by
+    a_c(theta)^(-k/2), the symbol of the scaled constant-coupling operator,
+    then scales each crop to unit RMS; k = 0 only rescales."""
+    from exploringsycl_gb300.learned import smooth_probes
+    rng = np.random.default_rng(5)
+    noise = rng.standard_normal((3, 32, 48)).astype(np.float32)
+    c = np.array([3.4, 100.0, 13000.0])
+    flat = smooth_probes(noise, c, 0.0)
+    scale = np.sqrt(np.mean(noise.astype(np.float64) ** 2, axis=(1, 2), keepdims=True))
+    assert np.allclose(flat, noise / scale, rtol=1e-5, atol=1e-6)
+    for k in (0.5, 1.0):
+        r = smooth_probes(noise, c, k).astype(np.float64)
+        assert np.allclose(np.sqrt(np.mean(r * r, axis=(1, 2))), 1.0, rtol=1e-5)
+        ty = 2 * np.pi * np.fft.fftfreq(32)[:, None]
+        tx = 2 * np.pi * np.fft.fftfreq(48)[None, :]
+        for b in range(3):
+            a = (1 + 2 * c[b] * (2 - np.cos(ty) - np.cos(tx))) / (1 + 4 * c[b])
+            ratio = np.fft.fft2(r[b]) / np.fft.fft2(noise[b].astype(np.float64))
+            gain = ratio / a ** (-0.5 * k)  # one real constant: the RMS scaling
+            assert np.allclose(gain, gain[0, 0].real, rtol=1e-4, atol=0)
+            # the lowest frequencies gain the most, the highest the least
+            assert abs(ratio[0, 0]) > abs(ratio[16, 24])
