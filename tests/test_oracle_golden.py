@@ -60,6 +60,18 @@ def test_tabulated_temperatures_pass(name):
     assert abs(100.0 * act / exp - 100.0) < 0.001
 
 
+def test_thesis_call_count_of_bm2():
+    """The thesis counts 2345 cg_calc_w calls over the 10 steps of bm2, the
+    five-state deck at 250^2 (Exploring_The_Performance_Portability_Of_SYCL.pdf,
+    section 4.1.4). The driver prints "CG: tt iterations" with tt the step at
+    which it stopped, one less than its calls of a converged solve
+    (TeaLeaf/drivers/cg_driver.c:18-27), so the reference driver's golden run
+    with the oracle kernels makes exactly that many calls."""
+    iters = GOLDEN["runs"]["five_state_250x10"]["iterations"]
+    assert len(iters) == 10
+    assert sum(iters) + len(iters) == 2345
+
+
 def test_full_size_tabulated_deck():
     """The largest deck the reference tabulates, 4096^2 for one step
     (TeaLeaf/tea.problems:2): the reference's driver with the oracle kernels
