@@ -4,8 +4,8 @@ Runs the reference's own, unchanged TeaLeaf host driver (compiled from the
 reference sources by `make -C oracle ref`, linked with the CPU oracle
 kernels) on a set of decks, and records what it prints: CG step counts,
 per-step error, the full-precision field summaries and the pass/fail check.
-The 4096^2 and 4000^2 decks of TeaLeaf/tea.problems are recorded apart
-("full_size"): their CPU runs take about three and twenty-five minutes.
+The larger decks of TeaLeaf/tea.problems are recorded apart ("full_size"):
+their CPU runs take up to 25 minutes (4000^2 x 10).
 Also records the final field summaries that the reference's Fortran runs
 printed in TeaLeaf/Benchmarks/tea_bm_{1,2,3}.out (line 173 of each).
 
@@ -69,11 +69,14 @@ DECKS = {
     "strip_40x1x2": dk.Deck(40, 1, _BG, end_step=2),
 }
 
-# The largest decks that the reference tabulates (TeaLeaf/tea.problems:2,5), the
-# second also the thesis's bm5 (Exploring_The_Performance_Portability_Of_SYCL.pdf,
-# section 4.1.4): kept apart from DECKS because their CPU runs take minutes.
-FULL_SIZE = {"five_state_4096x1": dk.five_state(4096, end_step=1),
-             "five_state_4000x10": dk.five_state(4000, end_step=10)}
+# The other decks that the reference tabulates (TeaLeaf/tea.problems:1,3,5,9,2),
+# 4000^2 x 10 also the thesis's bm5 (Exploring_The_Performance_Portability_Of_SYCL.pdf,
+# section 4.1.4): kept apart from DECKS because their CPU runs take up to minutes.
+FULL_SIZE = {"five_state_512x20": dk.five_state(512, end_step=20),
+             "five_state_1024x20": dk.five_state(1024, end_step=20),
+             "five_state_1000x10": dk.five_state(1000, end_step=10),
+             "five_state_4000x10": dk.five_state(4000, end_step=10),
+             "five_state_4096x1": dk.five_state(4096, end_step=1)}
 
 FORTRAN_OUT = {1: "tea_bm_1.out", 2: "tea_bm_2.out", 3: "tea_bm_3.out"}
 

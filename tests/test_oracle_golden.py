@@ -60,6 +60,24 @@ def test_tabulated_temperatures_pass(name):
     assert abs(100.0 * act / exp - 100.0) < 0.001
 
 
+def test_every_tabulated_deck_passes():
+    """All nine entries of TeaLeaf/tea.problems (the five-state deck from
+    10^2 x 10 steps to 4096^2 x 1): the reference's driver with the oracle
+    kernels passes each, with the final temperature within 1e-9 of the
+    table (the driver itself checks to 0.001 %; 64^2 x 1 differs by 2.7e-10,
+    the others by 1e-12 or less)."""
+    from .drivers import PROBLEMS
+    rows = [ln.split() for ln in PROBLEMS.splitlines() if ln.strip()]
+    assert len(rows) == 9
+    for x, y, steps, temp in rows:
+        assert x == y
+        name = f"five_state_{x}x{steps}"
+        rec = GOLDEN["runs"].get(name) or GOLDEN["full_size"][name]
+        assert rec["passed"] is True, name
+        assert len(rec["iterations"]) == int(steps), name
+        assert math.isclose(rec["summaries"][-1][3], float(temp), rel_tol=1e-9), name
+
+
 def test_thesis_call_count_of_bm2():
     """The thesis counts 2345 cg_calc_w calls over the 10 steps of bm2, the
     five-state deck at 250^2 (Exploring_The_Performance_Portability_Of_SYCL.pdf,

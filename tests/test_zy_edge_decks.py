@@ -1,9 +1,9 @@
 """Edge cases under the TeaLeaf host driver on the GPU, against what the
 reference's own driver printed with the oracle kernels: a point state that
 paints one cell, a CG solve stopped by max_iters before it converges,
-interiors one cell wide (narrower than the halo), and the largest decks that
-the reference tabulates (4096^2, one step of 4996 CG iterations, whose
-reductions run three levels of partial sums; 4000^2 for ten steps). CG step counts, per-step
+interiors one cell wide (narrower than the halo), and the larger decks that
+the reference tabulates (up to 4096^2, one step of 4996 CG iterations, whose
+reductions run three levels of partial sums, and 4000^2 for ten steps). CG step counts, per-step
 errors and full-precision field summaries must agree bit for bit, with the
 whole timestep solved on the device and replayed (fused) and, for the small
 decks, with one kernel per driver call (stepwise).
@@ -48,8 +48,9 @@ def test_edge_decks_match_reference_driver_golden(name, mode, tmp_path, backend_
 
 @pytest.mark.parametrize("name", sorted(GOLDEN["full_size"]))
 def test_full_size_tabulated_deck_matches_reference_driver_bitwise(name, tmp_path, backend_built):
-    """The reference's tabulated decks at full size: 4096^2 for one step and
-    bm5, 4000^2 for ten steps (42307 CG steps in all)."""
+    """The reference's tabulated decks recorded apart: 512^2 x 20 steps,
+    1000^2 x 10, 1024^2 x 20, bm5 (4000^2 x 10, 42307 CG steps in all) and
+    4096^2 x 1."""
     g = GOLDEN["full_size"][name]
     r = run_driver(DRIVER_EXE, _TextDeck(g["deck"]), tmp_path)
     assert r.returncode == 0, r.stdout[-1000:]
