@@ -15,6 +15,9 @@ tl_net_*); Python only orchestrates.
   from material interfaces (the default: see train_cli).
 * train(): Adam on random crops of those residuals, with the loss
   sum ||A M^-1 r - r||^2 / sum ||r||^2 over the batch, on the crop interiors.
+  Residual crops may be replaced by white-noise probes, optionally smoothed
+  by the operator's symbol (smooth_probes) so that the loss weighs the low
+  frequencies, where CG converges slowly, more.
 * Weights file: a .npz with the FP32 weight vector, the layout version and a
   SHA-256 of the weight bytes, checked on load.
 """
