@@ -434,12 +434,15 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
 
   if (prm->method == TL_METHOD_CG64) {
     int steps = 0;
-    rc = tl_internal_cg64_loop(ctx, x, y, hd, target, prm->max_inner, p, r, u, w, kx, ky, rro,
-                               nullptr, nullptr, &steps);
-    if (rc != TL_OK) return rc;
+    /* r = 0 (a zero right-hand side) is solved already; CG would form 0/0. */
+    if (rro > 0.0) {
+      rc = tl_internal_cg64_loop(ctx, x, y, hd, target, prm->max_inner, p, r, u, w, kx, ky,
+                                 rro, nullptr, nullptr, &steps);
+      if (rc != TL_OK) return rc;
+    }
     rep->inner_steps = steps;
     rep->outer_steps = 1;
-    rep->inner_kernel_ms = ctx->last_solve.kernel_ms;
+    rep->inner_kernel_ms = rro > 0.0 ? ctx->last_solve.kernel_ms : 0.0f;
     double rn = 0.0;
     double* uu[1] = {u};
     rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu, 1);
