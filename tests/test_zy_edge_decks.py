@@ -3,10 +3,11 @@ reference's own driver printed with the oracle kernels: a point state that
 paints one cell, a CG solve stopped by max_iters before it converges,
 interiors one cell wide (narrower than the halo), and the larger decks that
 the reference tabulates (up to 4096^2, one step of 4996 CG iterations, whose
-reductions run three levels of partial sums, and 4000^2 for ten steps). CG step counts, per-step
-errors and full-precision field summaries must agree bit for bit, with the
-whole timestep solved on the device and replayed (fused) and, for the small
-decks, with one kernel per driver call (stepwise).
+reductions run three levels of partial sums, and 4000^2 for ten steps). CG
+step counts, per-step errors and full-precision field summaries must agree
+bit for bit, with the whole timestep solved on the device and replayed
+(fused) and, for the small decks, with one kernel per driver call
+(stepwise).
 
 Collected after the other GPU modules and before the allocation-free entry
 point's, so that a run stopping at the first failure has run those first."""
