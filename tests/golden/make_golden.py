@@ -7,10 +7,10 @@ per-step error, the full-precision field summaries and the pass/fail check.
 The larger decks of TeaLeaf/tea.problems are recorded apart ("full_size"):
 their CPU runs take up to 25 minutes (4000^2 x 10).
 Also records the final field summaries that the reference's Fortran runs
-printed in TeaLeaf/Benchmarks/tea_bm_{1,2,3}.out (line 173 of each).
+printed in TeaLeaf/Benchmarks/tea_bm_{1..5}.out (FORTRAN_OUT).
 
 Needs the reference sources (default /root/reference/TeaLeaf, or TEALEAF_REF).
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--fortran-only]
 """
 from __future__ import annotations
 
@@ -78,22 +78,34 @@ FULL_SIZE = {"five_state_512x20": dk.five_state(512, end_step=20),
              "five_state_4000x10": dk.five_state(4000, end_step=10),
              "five_state_4096x1": dk.five_state(4096, end_step=1)}
 
-FORTRAN_OUT = {1: "tea_bm_1.out", 2: "tea_bm_2.out", 3: "tea_bm_3.out"}
+# The step-10 field summary of each Fortran benchmark run: file and line
+# ("step: 10 volume mass density energy u").
+FORTRAN_OUT = {1: ("tea_bm_1.out", 173), 2: ("tea_bm_2.out", 173), 3: ("tea_bm_3.out", 173),
+               4: ("tea_bm_4.out", 173), 5: ("tea_bm_5.out", 185)}
 
 
 def fortran_summaries() -> dict:
     out = {}
-    for bm, name in FORTRAN_OUT.items():
+    for bm, (name, lineno) in FORTRAN_OUT.items():
         text = (oracle.REFERENCE_SOURCES / "Benchmarks" / name).read_text().splitlines()
-        line = text[172]  # line 173: "step: 10 volume mass density energy u"
+        line = text[lineno - 1]
+        assert line.split()[:2] == ["step:", "10"], (name, lineno, line)
         vals = [float(v.replace("D", "E")) for v in line.split()[2:]]
-        out[f"tea_bm_{bm}"] = {"source": f"TeaLeaf/Benchmarks/{name}:173",
+        out[f"tea_bm_{bm}"] = {"source": f"TeaLeaf/Benchmarks/{name}:{lineno}",
                                "volume": vals[0], "mass": vals[1], "density": vals[2],
                                "energy": vals[3], "u": vals[4]}
     return out
 
 
 def main() -> None:
+    path = Path(__file__).with_name("reference_driver_runs.json")
+    if "--fortran-only" in sys.argv[1:]:
+        # refresh the Fortran summaries alone, keeping the recorded runs
+        out = json.loads(path.read_text())
+        out["fortran_step10"] = fortran_summaries()
+        path.write_text(json.dumps(out, indent=1))
+        print(f"wrote {path}")
+        return
     oracle.build(with_reference=True)
     runs, full = {}, {}
     with tempfile.TemporaryDirectory() as tmp:
@@ -110,7 +122,6 @@ def main() -> None:
            "driver": "reference TeaLeaf host driver (TeaLeaf/*.c, drivers/*.c, -DNO_MPI) "
                      "linked with oracle/tl_oracle.c",
            "runs": runs, "full_size": full, "fortran_step10": fortran_summaries()}
-    path = Path(__file__).with_name("reference_driver_runs.json")
     path.write_text(json.dumps(out, indent=1))
     print(f"wrote {path}")
 
