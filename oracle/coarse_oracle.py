@@ -78,6 +78,30 @@ def two_level_apply(K: np.ndarray, s: np.ndarray, Ac_inv: np.ndarray, r: np.ndar
     return nn.apply_collapsed(K, r, s) + prolong(e, blk)
 
 
+def coarse_cg(Ac: np.ndarray, rhs: np.ndarray, steps: int) -> np.ndarray:
+    """An inexact coarse solve: `steps` steps of Jacobi-preconditioned CG on
+    Ac e = rhs from e = 0. It is not linear in rhs, so the outer iteration
+    must be flexible PCG (fpcg)."""
+    d = np.diag(Ac)
+    e = np.zeros_like(rhs)
+    r = rhs.copy()
+    z = r / d
+    p = z.copy()
+    rz = float(r @ z)
+    for _ in range(steps):
+        if rz == 0.0:
+            break
+        q = Ac @ p
+        alpha = rz / float(p @ q)
+        e += alpha * p
+        r -= alpha * q
+        z = r / d
+        rz_new = float(r @ z)
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return e
+
+
 def fpcg(apply_a, b: np.ndarray, apply_m, tol: float = 1e-10,
          max_steps: int = 100000) -> tuple[np.ndarray, int]:
     """Flexible PCG (beta = (r_new . z_new - r_old . z_new) / (r_old . z_old)),

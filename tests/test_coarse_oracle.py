@@ -88,3 +88,27 @@ def test_coarse_level_cuts_the_steps_of_the_learned_pcg():
     assert two_level < 0.5 * learned, (learned, two_level)
     for x in (x1, x2):
         assert np.linalg.norm(a(x) - b) <= 1e-9 * np.linalg.norm(b)
+
+
+def test_inexact_coarse_solve_inside_flexible_pcg():
+    """A few Jacobi-PCG steps on the coarse system instead of its inverse (a
+    preconditioner that is not linear in r): flexible PCG still reaches the
+    tolerance, in fewer steps than without the coarse level."""
+    rng = np.random.default_rng(3)
+    H = W = 64
+    blk = 4
+    kx, ky = _couplings(rng, H, W, 2, 4)
+    a = _apply_a(kx, ky)
+    s = 1.0 / np.sqrt(_diagonal(kx, ky))
+    K = _stencil()
+    Ac = co.coarse_operator(kx, ky, blk)
+    b = rng.standard_normal((H, W))
+
+    def inexact(r):
+        e = co.coarse_cg(Ac, co.restrict(r, blk).ravel(), 5).reshape(H // blk, W // blk)
+        return nn.apply_collapsed(K, r, s) + co.prolong(e, blk)
+
+    _, learned = co.fpcg(a, b, lambda r: nn.apply_collapsed(K, r, s))
+    x, two_level = co.fpcg(a, b, inexact)
+    assert two_level < learned, (learned, two_level)
+    assert np.linalg.norm(a(x) - b) <= 1e-9 * np.linalg.norm(b)
