@@ -23,7 +23,7 @@
  *  - Scalars follow the reference: rro and pw are accumulated (+=), while
  *    rrn, norm, error and the field summary are overwritten
  *    (TeaLeaf/c_kernels/sycl/cg.cpp:133,194,253; solver_methods.cpp:116;
- *    jacobi.cpp:241; field_summary.cpp:394-397).
+ *    jacobi.cpp:116; field_summary.cpp:147-150).
  *  - Reductions are deterministic and follow the reference's summation
  *    order exactly (64-wide pairwise trees over consecutive linear cells,
  *    then over partial sums: TeaLeaf/c_kernels/sycl/cg.cpp:113-126,
@@ -410,7 +410,7 @@ int tl_ppcg_inner_iteration(tl_context* ctx, int x, int y, int halo_depth,
  * up after budget_ms (at most 1000) and records TL_ERR_TIMEOUT, which is
  * returned in *status; the context stays usable. No counterpart in the
  * reference (its host waits are unbounded, TeaLeaf/c_kernels/sycl/
- * sycl_shared.hpp:358). */
+ * sycl_shared.hpp:77, a blocking host accessor). */
 int tl_selftest_barrier_timeout(tl_context* ctx, int budget_ms, int* status);
 
 #ifdef __cplusplus

@@ -18,7 +18,9 @@ ORACLE_DIR = Path(__file__).resolve().parent
 LIB = ORACLE_DIR / "_build" / "libtl_oracle.so"
 DRIVER = ORACLE_DIR / "_build" / "tealeaf_oracle"
 REF_DRIVER = ORACLE_DIR / "_ref" / "tealeaf_ref"
-REFERENCE_SOURCES = Path(os.environ.get("TEALEAF_REF", "/root/reference/TeaLeaf"))
+# The reference sources: TEALEAF_REF, else a TeaLeaf tree beside this repository.
+REFERENCE_SOURCES = Path(os.environ.get("TEALEAF_REF",
+                                        ORACLE_DIR.parent.parent / "reference" / "TeaLeaf"))
 
 
 class OrcState(C.Structure):

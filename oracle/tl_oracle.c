@@ -60,7 +60,7 @@ static double orc_tree64(double* a) {
 }
 
 /* Second stage: reduce n partial sums level by level with the 64-wide tree
- * (TeaLeaf/c_kernels/sycl/sycl_shared.hpp:316-360). Consumes `part`. */
+ * (TeaLeaf/c_kernels/sycl/sycl_shared.hpp:35-79). Consumes `part`. */
 static double reduce_levels(double* part, long n) {
   double* next = (double*)malloc(sizeof(double) * (size_t)((n + WG - 1) / WG + 1));
   while (n != 1) {

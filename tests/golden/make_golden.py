@@ -9,7 +9,7 @@ their CPU runs take up to 25 minutes (4000^2 x 10).
 Also records the final field summaries that the reference's Fortran runs
 printed in TeaLeaf/Benchmarks/tea_bm_{1..5}.out (FORTRAN_OUT).
 
-Needs the reference sources (default /root/reference/TeaLeaf, or TEALEAF_REF).
+Needs the reference sources (TEALEAF_REF, default ../reference/TeaLeaf beside the repository).
 Usage: python tests/golden/make_golden.py [--fortran-only]
 """
 from __future__ import annotations

@@ -10,7 +10,8 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("TEALEAF_REF", "/root/reference/TeaLeaf"))
+REF = Path(os.environ.get("TEALEAF_REF",
+                         Path(__file__).resolve().parents[2] / "reference" / "TeaLeaf"))
 
 
 @pytest.mark.skipif(not REF.is_dir(), reason="reference sources not present")
