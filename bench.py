@@ -12,27 +12,33 @@ same timesteps are also solved, under the same stop rule, with plain FP64 CG
 in both arithmetic contracts (exact / fused multiply-add) and with the
 mixed-precision Jacobi-PCG solver (the `compare` list). A step is one
 timestep (TeaLeaf/diffuse.c:23-78): halo update, the solve, residual / norm /
-finalise. Timesteps follow one another (warm-up steps are timesteps 1..W).
-`--solver plain --deck two-state` is the drop-in configuration: the
-reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000
+finalise, and the field summary. Timesteps follow one another: the W warm-up
+steps are timesteps 1..W and the K timed steps are timesteps W+1..W+K, in
+every arm. `--solver plain --deck two-state` is the drop-in configuration:
+the reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000
 (`--fp64 fused` for the fused multiply-add contract).
 
 Reported:
   value      device time per timestep (CUDA events on the library's stream,
              inputs resident in HBM; every field is larger than L2)
-  e2e        the same timestep through the C ABI with host buffers: density
-             and energy copied in from pinned host memory, energy and the
-             field summary copied back, inside the timed region
+  e2e        the same K timesteps again, from the same starting state,
+             through the C ABI with host buffers: density and energy copied
+             in from pinned host memory, energy copied back, inside the
+             timed region (host wall clock, one synchronisation per step)
+  iters_per_s  solver steps (CG or inner PCG steps) per second of `value`
   roofline   the dominant kernel (the persistent inner FP32 kernel of the
              mixed solver, or the FP64 CG kernel for plain/cg64): algorithmic
              bytes / kernel time against the measured HBM copy bandwidth; for
              the FP64 kernel also FP64 instructions / s against the FP64 peak
-  cpu_baseline  the CPU oracle (restatement of the reference's kernels) on
-             this host's cores: plain FP64 CG steps of timestep 1 timed and
-             scaled by the CG step count of each timestep under the same stop
-             rule (bit-identical on CPU and GPU)
---impl reference times only that CPU path (the reference's algorithm: plain
-FP64 CG) as a bounded sample per step.
+  solve.error_vs_fp64  the headline solver's u and field summary against
+             plain FP64 CG (exact contract, bit-identical to the CPU oracle)
+             on the same timesteps
+  cpu_baseline  one whole timestep (W+1) of plain FP64 CG on the CPU oracle
+             (restatement of the reference's kernels) on this host's cores,
+             started from the GPU's FP64 CG state at the start of the timed
+             window, which the oracle would have computed bit for bit
+--impl reference times that CPU path alone through whole timesteps: 1..W
+untimed, W+1..W+K timed (the same window as the GPU arm).
 
 Multi-GPU: replicas only (one independent chunk per GPU); value is the
 whole-job time per timestep (max over ranks / timesteps of all ranks).
@@ -40,7 +46,6 @@ whole-job time per timestep (max over ranks / timesteps of all ranks).
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import json
 import os
 import statistics
@@ -49,6 +54,8 @@ import sys
 import tempfile
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -80,10 +87,9 @@ NCU_BYTES_PER_CELL_STEP = {
     ("inner_cg_kernel", None): 51.3,           # profiles/inner_cg_mixed_jacobi_4096.txt
     ("lpcg_kernel", None): 51.3,               # profiles/lpcg_learned_4096.txt
 }
-ITER_FIXTURES = {"two-state": ROOT / "tests" / "golden" / "cg_iterations_two_state_4096.json",
-                 "random": ROOT / "tests" / "golden" / "cg_iterations_random_4096.json"}
 RANDOM_SEED = 1
 REL_TOL = 1e-10
+MAX_ITERS = 10000
 
 
 def load_peaks() -> dict:
@@ -146,9 +152,6 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-MAX_ITERS = 10000
-
-
 def deck_for(size: int, kind: str = "random"):
     from exploringsycl_gb300 import deck as dk
     if kind == "two-state":
@@ -159,7 +162,7 @@ def deck_for(size: int, kind: str = "random"):
 
 def stop_rule(solver: str) -> str:
     if solver == "plain":
-        return "sqrt(|rr|) < 1e-15 (the reference's absolute rule), max_iters 10000"
+        return f"sqrt(|rr|) < 1e-15 (the reference's absolute rule), max_iters {MAX_ITERS}"
     return f"FP64 true residual ||u0 - A u|| <= {REL_TOL:g} ||u0||"
 
 
@@ -181,89 +184,73 @@ def config_for(args, steps_per_timestep=None) -> dict:
             "cells": args.size * args.size, "halo_depth": 2, "dt": 0.004,
             "deck": args.deck, "solver": args.solver, "stop": stop_rule(args.solver),
             "max_iters": MAX_ITERS,
-            "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2)",
+            "timed_timesteps": [args.warmup + 1, args.warmup + args.steps],
+            "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2)"
+                  if args.size >= 4096 else "fields smaller than L2 at this size",
             "cg_steps_per_timestep": steps_per_timestep}
 
 
 # ----------------------------------------------------------------- CPU side
 
-def cpu_sample(size: int, iters: int, kind: str = "random", threads: int | None = None) -> dict:
-    """Times `iters` CG steps of timestep 1 with the CPU oracle."""
-    from oracle import oracle
-    oracle.build(with_reference=False)
-    L = oracle.lib()
-    if threads:
-        L.orc_set_num_threads(threads)
-    ch = oracle.OracleChunk(deck_for(size, kind))
-    # timestep 1 set-up, as in cg_timestep
-    x, y, hd = ch.x, ch.y, ch.hd
-    rx, ry = ch.rx_ry()
-    ch.halos(["energy", "density"], 2)
-    rro = C.c_double(0.0)
-    L.orc_cg_init_u(x, y, ch.coefficient, ch.p("p"), ch.p("r"), ch.p("u"), ch.p("w"),
-                    ch.p("density"), ch.p("energy"))
-    L.orc_cg_init_k(x, y, hd, ch.p("w"), ch.p("kx"), ch.p("ky"), rx, ry)
-    L.orc_cg_init_others(x, y, hd, ch.p("kx"), ch.p("ky"), ch.p("p"), ch.p("r"), ch.p("u"),
-                         ch.p("w"), C.byref(rro))
-    ch.halos(["u", "p"], 1)
-    L.orc_copy_u(x, y, hd, ch.p("u"), ch.p("u0"))
-    r = rro.value
-    t0 = time.perf_counter()
-    for _ in range(iters):
-        pw = C.c_double(0.0)
-        L.orc_cg_calc_w(x, y, hd, ch.p("w"), ch.p("p"), ch.p("kx"), ch.p("ky"), C.byref(pw))
-        alpha = r / pw.value
-        rrn = C.c_double(0.0)
-        L.orc_cg_calc_ur(x, y, hd, ch.p("u"), ch.p("r"), ch.p("p"), ch.p("w"), alpha,
-                         C.byref(rrn))
-        L.orc_cg_calc_p(x, y, hd, rrn.value / r, ch.p("p"), ch.p("r"))
-        r = rrn.value
-        ch.halos(["u", "p"], 1)
-    dt = time.perf_counter() - t0
-    return {"s_per_iter": dt / iters, "cores": L.orc_num_threads(), "iters": iters}
+class CpuTimesteps:
+    """Plain FP64 CG timesteps on the CPU oracle (a restatement of the
+    reference's kernels, OpenMP over the host's cores), each one whole: the
+    halo update, cg_init, the CG loop under the arm's stop rule, residual /
+    norm / finalise and the field summary, as the GPU steps do."""
 
+    def __init__(self, args, threads: int | None = None):
+        from oracle import oracle
+        oracle.build(with_reference=False)
+        self.L = oracle.lib()
+        if threads:
+            self.L.orc_set_num_threads(threads)
+        self.cores = self.L.orc_num_threads()
+        self.plain = args.solver == "plain"
+        self.contract = args.fp64 if args.solver in ("plain", "cg64") else "exact"
+        self.chunk = oracle.OracleChunk(deck_for(args.size, args.deck))
 
-def fixture_iterations(size: int, kind: str) -> list[int] | None:
-    """Plain FP64 CG step counts of consecutive timesteps, recorded from a
-    GPU run (the GPU's FP64 CG is bit-identical to the oracle's)."""
-    p = ITER_FIXTURES[kind]
-    if p.exists():
-        d = json.loads(p.read_text())
-        if d.get("size") == size:
-            return d["cg_steps"]
-    return None
+    def load_energy(self, energy: np.ndarray) -> None:
+        """Starts from another run's state: energy is the only field that a
+        timestep carries to the next (density and energy0 do not change)."""
+        self.chunk.f["energy"][:] = energy
+
+    def step(self) -> dict:
+        t0 = time.perf_counter()
+        if self.plain:
+            steps = self.chunk.cg_timestep(contract=self.contract)
+        else:
+            steps = self.chunk.cg_timestep(rel_tol=REL_TOL, contract=self.contract)
+        summary = self.chunk.summary()
+        return {"s": time.perf_counter() - t0, "cg_steps": steps, "summary": summary}
 
 
 def run_reference(args, rank: int, world: int) -> None:
-    """CPU implementation of the reference's algorithm (the oracle port)."""
+    """The reference's algorithm (plain FP64 CG, the CPU oracle) through
+    whole timesteps: 1..W untimed, W+1..W+K timed."""
     if rank != 0:
         return
-    iters_per_ts = fixture_iterations(args.size, args.deck)
-    if iters_per_ts is None:
-        print(json.dumps({"impl": "reference", "unavailable":
-                          f"no CG step counts for {args.size}^2 timesteps recorded yet"}))
-        return
-    first = args.warmup
-    ts_steps = iters_per_ts[first:first + args.steps] or iters_per_ts[-args.steps:]
-    mean_steps = statistics.mean(ts_steps)
-    per_step = []
-    cores = None
-    for k in range(args.warmup + args.steps):
-        s = cpu_sample(args.size, args.ref_iters, args.deck)
-        cores = s["cores"]
-        if k >= args.warmup:
-            per_step.append(s["s_per_iter"])
-    s_per_iter = statistics.mean(per_step)
-    value = s_per_iter * mean_steps
+    cpu = CpuTimesteps(args)
+    warm = [cpu.step() for _ in range(args.warmup)]
+    t0 = time.perf_counter()
+    timed = [cpu.step() for _ in range(args.steps)]
+    total = time.perf_counter() - t0
+    value = total / args.steps
+    steps = [s["cg_steps"] for s in timed]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(config_for(args, ts_steps), solver="plain FP64 CG (CPU oracle)"),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.ref_iters} CG steps of timestep 1 per step, "
-                                   f"scaled by {mean_steps:.1f} CG steps per timestep"},
+        "config": dict(config_for(args, [s["cg_steps"] for s in warm + timed]),
+                       solver="plain FP64 CG (CPU oracle, restatement of the reference's "
+                              "c_kernels/sycl semantics)"),
+        "iters_per_s": sum(steps) / total,
+        "per_timestep_s": [s["s"] for s in timed],
+        "summary_last": timed[-1]["summary"] if timed else None,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": "port",
+                         "sample": f"whole timesteps {args.warmup + 1}..{args.warmup + args.steps}"
+                                   f" ({sum(steps)} CG steps), after timesteps 1..{args.warmup}"
+                                   " untimed"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -286,7 +273,8 @@ class Stepper:
 
     def __init__(self, args, solver: str, ctx, contract: str | None = None):
         from exploringsycl_gb300.chunk import GpuChunk
-        ctx.set_fp64_contract(contract or args.fp64)
+        self.contract = contract or args.fp64
+        ctx.set_fp64_contract(self.contract)
         self.solver = solver
         self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
         self.ctx = ctx
@@ -300,39 +288,92 @@ class Stepper:
             self.net = Net(ctx, w)
 
     def step(self) -> dict:
-        """Runs one timestep; returns the dominant kernel's time and steps."""
+        """Runs one timestep and its field summary; returns the dominant
+        kernel's time and steps."""
         if self.solver == "plain":
             steps = self.chunk.cg_timestep()
             st = self.ctx.solve_stats()
-            return {"kernel_ms": st.kernel_ms, "kernel_steps": steps, "cg_steps": steps}
-        rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL, inner_tol=self.inner_tol,
-                                        learned=self.net, max_inner=self.max_inner,
-                                        max_outer=self.max_outer)
-        return {"kernel_ms": rep["inner_kernel_ms"],
-                "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
-                "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
+            out = {"kernel_ms": st.kernel_ms, "kernel_steps": steps, "cg_steps": steps}
+        else:
+            rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL,
+                                            inner_tol=self.inner_tol, learned=self.net,
+                                            max_inner=self.max_inner, max_outer=self.max_outer)
+            out = {"kernel_ms": rep["inner_kernel_ms"],
+                   "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
+                   "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
+        out["summary"] = self.chunk.summary()
+        return out
+
+    def energy(self) -> np.ndarray:
+        return self.chunk.read("energy")
+
+    def close(self) -> None:
+        if self.net is not None:
+            self.net.close()
+        self.chunk.close()
 
 
 def timed_steps(stepper, steps: int, stream, barrier, sample_clocks: bool, device: int):
+    """K timesteps bracketed by a barrier and a device synchronisation on
+    both sides; CUDA events on the library's stream between the timesteps
+    give the total and each timestep's device time."""
     import torch
     barrier()
     torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
     sampler = ClockSampler(device) if sample_clocks else None
     if sampler:
         sampler.start()
     launches0 = stepper.ctx.launches()
     per = []
-    ev0.record(stream)
-    for _ in range(steps):
+    evs[0].record(stream)
+    for k in range(steps):
         per.append(stepper.step())
-    ev1.record(stream)
-    ev1.synchronize()
+        evs[k + 1].record(stream)
+    evs[-1].synchronize()
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
     barrier()
-    return ev0.elapsed_time(ev1), per, stepper.ctx.launches() - launches0, clocks
+    for k, p in enumerate(per):
+        p["device_ms"] = evs[k].elapsed_time(evs[k + 1])
+    return evs[0].elapsed_time(evs[-1]), per, stepper.ctx.launches() - launches0, clocks
+
+
+def e2e_steps(stepper, energy0: np.ndarray, steps: int, barrier) -> tuple[list[float], list]:
+    """The timed timesteps again, from the state they started from, through
+    the C ABI with host buffers: each step copies density and energy in from
+    pinned host memory, solves, and copies energy back (host wall clock)."""
+    import torch
+
+    from exploringsycl_gb300 import check
+    chunk, lib, ctx = stepper.chunk, stepper.ctx.lib, stepper.ctx
+    n = chunk.n
+    h_density = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    h_energy = torch.from_numpy(energy0).pin_memory()
+    check(lib.tl_copy_to_host(ctx.h, h_density.data_ptr(), chunk.f["density"], n), "copy")
+    barrier()
+    torch.cuda.synchronize()
+    times, summaries = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        check(lib.tl_copy_to_device(ctx.h, chunk.f["density"], h_density.data_ptr(), n), "copy")
+        check(lib.tl_copy_to_device(ctx.h, chunk.f["energy"], h_energy.data_ptr(), n), "copy")
+        out = stepper.step()
+        check(lib.tl_copy_to_host(ctx.h, h_energy.data_ptr(), chunk.f["energy"], n), "copy")
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        summaries.append(out["summary"])
+    barrier()
+    return times, summaries
+
+
+def rel_diff(a, b) -> float:
+    return abs(a - b) / abs(b) if b != 0 else abs(a - b)
+
+
+def interior(chunk, field: np.ndarray) -> np.ndarray:
+    hd = chunk.hd
+    return field.reshape(chunk.y, chunk.x)[hd:-hd, hd:-hd]
 
 
 def run_ours(args, rank: int, world: int, dist) -> None:
@@ -353,36 +394,20 @@ def run_ours(args, rank: int, world: int, dist) -> None:
 
     warm = [main.step() for _ in range(args.warmup)]
     torch.cuda.synchronize()
+    energy_w = main.energy()          # state at the start of the timed window
     total_ms, per, launches, clocks = timed_steps(main, args.steps, stream, barrier, True, local)
-
-    # e2e: host buffers in, results out, through the C ABI.
-    n = chunk.n
-    h_density = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    h_energy = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    h_out = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    lib = ctx.lib
-    lib.tl_copy_to_host(ctx.h, h_density.data_ptr(), chunk.f["density"], n)
-    lib.tl_copy_to_host(ctx.h, h_energy.data_ptr(), chunk.f["energy"], n)
-    e2e_times = []
-    summary = None
-    for _ in range(args.e2e_steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        lib.tl_copy_to_device(ctx.h, chunk.f["density"], h_density.data_ptr(), n)
-        lib.tl_copy_to_device(ctx.h, chunk.f["energy"], h_energy.data_ptr(), n)
-        main.step()
-        summary = chunk.summary()
-        lib.tl_copy_to_host(ctx.h, h_out.data_ptr(), chunk.f["energy"], n)
-        torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-        h_energy.copy_(h_out)
-    barrier()
+    u_main = interior(chunk, chunk.read("u"))
+    e2e_times, e2e_summaries = e2e_steps(main, energy_w, args.steps, barrier)
+    e2e_same = e2e_summaries == [p["summary"] for p in per]
 
     # The same timesteps with the other solvers under the same stop rule:
     # plain FP64 CG in both arithmetic contracts, and the mixed-precision
     # solvers not measured above.
     compare = []
-    if args.compare and args.solver != "plain":
+    fp64_ref = None          # (energy at W, per-step records, u at W+K) of exact FP64 CG
+    if args.solver in ("plain", "cg64") and args.fp64 == "exact":
+        fp64_ref = (energy_w, per, u_main)
+    if args.compare and args.solver not in ("plain", "cg64"):
         others = [("cg64", "exact", "plain FP64 CG (exact contract, bit-identical to the "
                                     "oracle), same stop rule"),
                   ("cg64", "fused", "plain FP64 CG (fused multiply-add contract), "
@@ -394,23 +419,23 @@ def run_ours(args, rank: int, world: int, dist) -> None:
             ctx2 = Context(device=local)
             other = Stepper(args, solver, ctx2, contract)
             cwarm = [other.step() for _ in range(args.warmup)]
+            torch.cuda.synchronize()
+            e_w = other.energy() if (solver, contract) == ("cg64", "exact") else None
             stream2 = torch.cuda.ExternalStream(ctx2.stream(), device=local)
             c_ms, c_per, _, _ = timed_steps(other, args.steps, stream2, barrier, False, local)
+            csteps = [p["cg_steps"] for p in c_per]
             entry = {"solver": label, "value": c_ms / 1e3 / args.steps, "unit": UNIT,
                      "cg_steps_per_timestep": [p["cg_steps"] for p in cwarm + c_per],
-                     "speedup_of_headline": (c_ms / args.steps) / (total_ms / args.steps)}
+                     "iters_per_s": sum(csteps) / (c_ms / 1e3),
+                     "speedup_of_headline": c_ms / total_ms}
             compare.append(entry)
-            if args.dump_iterations and solver == "cg64" and contract == "exact":
-                Path(args.dump_iterations).write_text(json.dumps(
-                    {"size": args.size, "deck": args.deck, "stop": stop_rule("cg64"),
-                     "cg_steps": entry["cg_steps_per_timestep"]}))
-            if other.net is not None:
-                other.net.close()
-            other.chunk.close()
+            if e_w is not None:
+                fp64_ref = (e_w, c_per, interior(other.chunk, other.chunk.read("u")))
+            other.close()
 
     total_ms, e2e_mean = max_over_ranks([total_ms, statistics.mean(e2e_times)], dist)
     if rank != 0:
-        ctx.close()
+        main.close()
         return
     value = total_ms / 1e3 / (args.steps * world)
     cells = args.size * args.size
@@ -440,6 +465,8 @@ def run_ours(args, rank: int, world: int, dist) -> None:
                      "fp64_gops": FP64_OPS_PER_CELL_STEP[args.fp64] * rate,
                      "fp64_pipe_gops": pipe, "fp64_peak_gops": FP64_PEAK_GOPS,
                      "fp64_pipe_frac": pipe / FP64_PEAK_GOPS})
+    n = chunk.n
+    timed_cg = [p["cg_steps"] for p in per]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
@@ -448,8 +475,11 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         "data": "synthetic",
         "config": config_for(args, [p["cg_steps"] for p in warm + per]),
         "e2e": {"value": e2e_mean / world, "unit": UNIT,
-                "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8 + 32,
-                "steps": args.e2e_steps},
+                "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8,
+                "steps": args.steps,
+                "timesteps": [args.warmup + 1, args.warmup + args.steps],
+                "same_results_as_timed": e2e_same},
+        "iters_per_s": sum(timed_cg) / (total_ms / 1e3 / world),
         "gpu_launches": launches,
         "roofline": roof,
         "clocks": clocks,
@@ -460,27 +490,45 @@ def run_ours(args, rank: int, world: int, dist) -> None:
             "outer_steps": [r["outer_steps"] for r in reports],
             "inner_steps": [r["inner_steps"] for r in reports],
             "fallback_events": sum(r["fallback_events"] for r in reports),
-            "final_rel_residual_max": max(r["final_rel_residual"] for r in reports),
-            "error_vs_fp64": "every timestep stops at an FP64 true residual <= 1e-10 relative "
-                             "(tests/test_gpu_mixed.py: u within 1e-7 of the FP64 oracle CG)"}
+            "final_rel_residual_max": max(r["final_rel_residual"] for r in reports)}
+    if fp64_ref is not None and args.solver not in ("plain", "cg64"):
+        _, ref_per, u_ref = fp64_ref
+        names = ("volume", "mass", "internal_energy", "temperature")
+        line.setdefault("solve", {})["error_vs_fp64"] = {
+            "against": "plain FP64 CG, exact contract (bit-identical to the CPU oracle), "
+                       "same deck, same stop rule, same timesteps",
+            "u_max_rel_at_last_timestep": float(np.max(np.abs(u_main - u_ref)) /
+                                                np.max(np.abs(u_ref))),
+            "summary_rel_max_over_timed_timesteps": {
+                nm: max(rel_diff(p["summary"][i], q["summary"][i])
+                        for p, q in zip(per, ref_per)) for i, nm in enumerate(names)}}
     if compare:
         line["compare"] = compare
     if not args.skip_cpu:
-        cpu = cpu_sample(args.size, args.cpu_iters, args.deck)
-        ref_steps = (compare[0]["cg_steps_per_timestep"][args.warmup:] if compare
-                     else [p["cg_steps"] for p in per])
-        mean_steps = statistics.mean(ref_steps)
+        # Timestep W+1 from the state of a GPU run that the oracle repeats bit
+        # for bit: the FP64 CG measured here, else the exact-contract compare.
+        if args.solver in ("plain", "cg64"):
+            start, gpu_step = energy_w, per[0]
+        elif fp64_ref is not None:
+            start, gpu_step = fp64_ref[0], fp64_ref[1][0]
+        else:
+            start, gpu_step = energy_w, None
+        cpu = CpuTimesteps(args)
+        cpu.load_energy(start)
+        s = cpu.step()
         line["cpu_baseline"] = {
-            "value": cpu["s_per_iter"] * mean_steps, "unit": UNIT, "cores": cpu["cores"],
-            "kind": "port",
-            "sample": f"{cpu['iters']} plain FP64 CG steps of timestep 1 on the CPU oracle, "
-                      f"scaled by {mean_steps:.1f} CG steps per timestep (same stop rule)"}
-    if args.dump_iterations and args.solver == "plain":
-        Path(args.dump_iterations).write_text(json.dumps(
-            {"size": args.size, "deck": args.deck, "stop": stop_rule("plain"),
-             "cg_steps": [p["cg_steps"] for p in warm + per], "summary_after": summary}))
+            "value": s["s"], "unit": UNIT, "cores": cpu.cores, "kind": "port",
+            "sample": f"timestep {args.warmup + 1} whole ({s['cg_steps']} CG steps), plain "
+                      f"FP64 CG on the CPU oracle ({cpu.contract} contract), from the GPU "
+                      "FP64 CG state at the start of the timed window",
+            "iters_per_s": s["cg_steps"] / s["s"]}
+        if gpu_step is not None:
+            line["cpu_baseline"].update({
+                "gpu_same_timestep_s": gpu_step["device_ms"] / 1e3,
+                "same_cg_steps_and_summary_as_gpu": (s["cg_steps"] == gpu_step["cg_steps"] and
+                                                     s["summary"] == gpu_step["summary"])})
     print(json.dumps(line))
-    chunk.close()
+    main.close()
 
 
 def main() -> None:
@@ -501,12 +549,8 @@ def main() -> None:
                     help="inner steps per refinement step (smaller only for profiling captures)")
     ap.add_argument("--max-outer", type=int, default=12)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
-                    help="skip the plain FP64 CG run of the same timesteps")
-    ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-iters", type=int, default=5)
-    ap.add_argument("--ref-iters", type=int, default=5)
+                    help="skip the other solvers' runs of the same timesteps")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--dump-iterations", default=None)
     ap.add_argument("--max-iters", type=int, default=10000,
                     help="cap on CG steps per timestep (smaller only for profiling captures)")
     args = ap.parse_args()

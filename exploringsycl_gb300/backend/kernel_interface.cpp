@@ -201,6 +201,21 @@ void run_kernel_initialise(Chunk* chunk, Settings* settings) {
   ext->ra_cap = (int)iters;
   ext->fused_cg = !env_is("TL_CG_MODE", "stepwise");
   read_backend_keys(settings, ext);
+  /* The whole-timestep paths solve this chunk alone. With more than one
+   * chunk (several per rank, or several ranks: TeaLeaf/initialise.c:34-38)
+   * the chunks' solves must be coupled through the driver's sums of pw and
+   * rrn over chunks and ranks, which only the step-wise kernels take part
+   * in: run-ahead gives way to them, and a solver replacement, which has no
+   * step-wise form, is refused. */
+  if (settings->num_chunks_per_rank > 1 || settings->num_ranks > 1) {
+    if (ext->replace_method >= 0) {
+      die(__LINE__, __FILE__,
+          "GB300 backend: gb300_solver / preconditioner_on solve one chunk; this run has "
+          "%d chunks per rank on %d ranks\n",
+          settings->num_chunks_per_rank, settings->num_ranks);
+    }
+    ext->fused_cg = 0;
+  }
 }
 
 /* TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:82-125 */
@@ -380,6 +395,14 @@ void run_cg_init(Chunk* chunk, Settings* settings, double rx, double ry,
            "rel_residual=%.6e device_ms=%.3f inner_gbs=%.1f\n",
            prm.method, rep.outer_steps, rep.inner_steps, rep.fallback_events,
            rep.fallback_steps, rep.final_rel_residual, rep.device_ms, gbs);
+    /* tl_solve falls back to FP64 CG whenever refinement does not reach the
+     * target; only an exhausted FP64 CG (max_iters steps) ends above it. */
+    if (!(rep.final_rel_residual <= prm.rel_tol)) {
+      die(__LINE__, __FILE__,
+          "GB300 backend: the solve ended at a relative residual of %.3e, above the "
+          "target %.3e, after %d fall-back steps (max_iters %d)\n",
+          rep.final_rel_residual, prm.rel_tol, rep.fallback_steps, settings->max_iters);
+    }
     /* One synthetic step with pw = 1, rrn = 0: the driver's loop ends at once. */
     *rro += 1.0;
     ext->ra_rro0 = 1.0;

@@ -500,11 +500,13 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
       if (rc != TL_OK) return rc;
       if (outer == 0) rep->initial_rel_residual = bnorm > 0 ? rn / bnorm : rn;
       rep->final_rel_residual = bnorm > 0 ? rn / bnorm : rn;
-      if (rn <= target || outer == prm->max_outer) break;
+      if (rn <= target) break;
       const bool stalled = outer > 0 && rn > prm->stall_factor * prev;
-      if (stalled || !(rn == rn)) {
-        /* Refinement no longer converges: finish with the exact FP64 CG
-         * from the current iterate. */
+      const bool exhausted = outer == prm->max_outer;
+      if (stalled || exhausted || !(rn == rn)) {
+        /* Refinement no longer converges, or has used its max_outer steps
+         * without reaching the target: finish with the exact FP64 CG from
+         * the current iterate. */
         rep->fallback_events++;
         int steps = 0;
         rc = tl_internal_cg64_from_iterate(ctx, x, y, hd, target, prm->max_fallback, p, r, u,

@@ -196,7 +196,10 @@ int tl_cg_calc_w(tl_context* ctx, int x, int y, int halo_depth, double* w,
  * 134,217,728 cells (32768 tiles of 4096 cells) are rejected with
  * TL_ERR_ARG. The first call on a device, with that device current, looks
  * up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture. Every call shares the array and leaves
+ * call before any stream capture. The address is kept for the life of the
+ * process: after cudaDeviceReset, or anything else that destroys the
+ * device's primary context, do not call this entry point again in that
+ * process. Every call shares the array and leaves
  * its last contents there (the ticket word is cleared at each call): calls
  * that overlap on the GPU race, so issue them on one stream or serialise
  * them. `stream` is the caller's cudaStream_t (NULL: the default stream).
@@ -259,7 +262,8 @@ typedef struct tl_solve_params {
                            0 selects the method's default (3e-6 for the
                            learned methods, 1e-5 otherwise) */
   int max_inner;        /* inner CG steps per outer step (CG64: total steps) */
-  int max_outer;        /* refinement steps */
+  int max_outer;        /* refinement steps; if they end above the target,
+                           FP64 CG finishes the solve as after a stall */
   double stall_factor;  /* an outer step must shrink the residual below
                            stall_factor x the previous one, else FP64 CG
                            finishes the solve from the current iterate */

@@ -315,7 +315,9 @@ int tl_solve(tl_context*, int, int, int, int, double, double, const tl_solve_par
   rep->outer_steps = 3;
   rep->inner_steps = 123;
   rep->initial_rel_residual = 1.0;
-  rep->final_rel_residual = 0.5 * prm->rel_tol;
+  /* FAKE_UNCONVERGED=1: a solve that ended above its target */
+  rep->final_rel_residual = getenv("FAKE_UNCONVERGED") ? 4.0 * prm->rel_tol
+                                                      : 0.5 * prm->rel_tol;
   rep->device_ms = 1.0f;
   rep->inner_kernel_ms = 0.5f;
   return TL_OK;

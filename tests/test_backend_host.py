@@ -178,3 +178,16 @@ def test_unknown_solver_name_is_refused(fake_driver, tmp_path):
     r, _ = _run(fake_driver, dk.two_state(16, end_step=1), tmp_path, TL_SOLVER="magic")
     assert r.returncode == 1
     assert "unknown solver 'magic'" in r.stdout
+
+
+def test_solve_that_ends_above_its_target_stops_the_run(fake_driver, tmp_path):
+    """A replacement solve whose final relative residual is above the target
+    (its FP64 fall-back ran out of max_iters) must not be reported to the
+    driver as converged."""
+    d = dk.two_state(16, end_step=1)
+    d.extra = ["gb300_solver mixed", "gb300_rel_tol 1e-10"]
+    r, calls = _run(fake_driver, d, tmp_path, FAKE_UNCONVERGED=1)
+    assert r.returncode == 1
+    assert "above the target 1.000e-10" in r.stdout
+    assert "tl_field_summary" not in _names(calls[calls.index(
+        next(c for c in calls if c.startswith("tl_solve"))):])

@@ -1,11 +1,13 @@
 """CPU: the reference arm of bench.py (the CPU implementation of the path,
 timed on the host cores) prints one JSON line with the keys of the bench
-contract, describing its own run in cpu_baseline and e2e."""
+contract, describing its own run in cpu_baseline and e2e; it times whole
+timesteps, and exactly the window W+1..W+K that the GPU arm times."""
 from __future__ import annotations
 
 import json
 import subprocess
 import sys
+import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -14,7 +16,7 @@ ROOT = Path(__file__).resolve().parents[1]
 def test_reference_arm_json_line():
     out = subprocess.run(
         [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
-         "--warmup", "3", "--ref-iters", "1"],
+         "--warmup", "3", "--size", "64"],
         cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     d = json.loads(out.stdout.strip().splitlines()[-1])
@@ -47,10 +49,36 @@ def test_reference_arm_under_torchrun_prints_one_line():
         [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
          "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
          "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3",
-         "--ref-iters", "1"],
+         "--size", "64"],
         cwd=ROOT, capture_output=True, text=True, timeout=900)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1, out.stdout[-2000:]
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_reference_arm_times_the_gpu_arms_window_whole(oracle_built):
+    """With W = 3 warm-up and K = 2 timed steps the arm runs timesteps 1..5,
+    times 4 and 5 whole (their CG step counts are those of the oracle's own
+    run of the same deck), and its claimed time fits in its wall clock."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    t0 = time.perf_counter()
+    out = subprocess.run(
+        [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "2",
+         "--warmup", "3", "--size", "64"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600)
+    wall = time.perf_counter() - t0
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    c = oracle_built.OracleChunk(bench.deck_for(64, "random"))
+    counts = [c.cg_timestep(rel_tol=bench.REL_TOL) for _ in range(5)]
+    assert d["config"]["cg_steps_per_timestep"] == counts
+    assert d["config"]["timed_timesteps"] == [4, 5]
+    assert "whole timesteps 4..5" in d["cpu_baseline"]["sample"]
+    assert f"({sum(counts[3:])} CG steps)" in d["cpu_baseline"]["sample"]
+    assert d["ms_per_step"] * d["steps"] / 1e3 <= wall
+    assert abs(d["iters_per_s"] - sum(counts[3:]) / (d["value"] * d["steps"])) <= \
+        1e-9 * d["iters_per_s"]
+    assert d["summary_last"] == list(c.summary())

@@ -1,7 +1,8 @@
 """Solver-replacement methods on the GPU: each reaches the relative FP64
 true-residual target; the exact FP64 method equals the oracle's CG with the
-same stop rule bit for bit; the mixed-precision methods agree with it to the
-accuracy the target implies; a stalled refinement falls back to FP64 CG.
+same stop rule bit for bit; the mixed-precision methods, the learned one
+included, agree with it to the accuracy the target implies (u and the four
+field-summary sums); a stalled or exhausted refinement falls back to FP64 CG.
 
 Tolerance for the mixed methods: both solutions satisfy
 ||u0 - A u|| <= 1e-10 ||u0||, so they differ by at most about
@@ -25,18 +26,28 @@ DECKS = {
 REL = 1e-10
 
 
-def _run(name, method, oracle_built, **kw):
+def _run(name, method, oracle_built, deck=None, **kw):
+    """Solves one timestep of the deck on the GPU with `method` and on the
+    CPU with the oracle's FP64 CG, both to the relative target REL."""
     from exploringsycl_gb300.chunk import GpuChunk
-    d = DECKS[name]()
+    d = deck if deck is not None else DECKS[name]()
     g = GpuChunk(d)
     c = oracle_built.OracleChunk(d)
+    net = None
     try:
+        if method == "mixed-learned":
+            from exploringsycl_gb300.learned import Net, load_weights
+            net = Net(g.ctx, load_weights()[0])
+            kw["learned"] = net
         rep = g.solve_timestep(method, rel_tol=REL, **kw)
         steps = c.cg_timestep(rel_tol=REL)
         return g, c, rep, steps
     except Exception:
         g.close()
         raise
+    finally:
+        if net is not None:
+            net.close()
 
 
 @pytest.mark.parametrize("name", list(DECKS))
@@ -51,21 +62,73 @@ def test_cg64_method_is_bitwise_oracle_cg(name, backend_built, oracle_built):
         g.close()
 
 
-@pytest.mark.parametrize("name", list(DECKS))
-@pytest.mark.parametrize("method", ["mixed", "mixed-jacobi"])
+def _assert_agree(g, c):
+    """u within 1e-7 of the oracle's (max norm, relative to max |u|), and
+    each field-summary sum (volume, mass, internal energy, temperature)
+    within 1e-7 relative."""
+    ug, uc = g.read("u"), c.f["u"]
+    hd = g.hd
+    ug = ug.reshape(g.y, g.x)[hd:-hd, hd:-hd]
+    uc = uc.reshape(c.y, c.x)[hd:-hd, hd:-hd]
+    assert np.max(np.abs(ug - uc)) <= 1e-7 * np.max(np.abs(uc))
+    for sg, sc in zip(g.summary(), c.summary()):
+        assert abs(sg - sc) <= 1e-7 * abs(sc), (g.summary(), c.summary())
+
+
+# The learned preconditioner needs an interior width divisible by 4; the
+# 75 x 90 deck is refused (TL_ERR_ARG) rather than solved.
+MIXED_CASES = [(n, m) for m in ("mixed", "mixed-jacobi", "mixed-learned") for n in DECKS
+               if not (m == "mixed-learned" and n == "random_odd_75x90")]
+
+
+@pytest.mark.parametrize("name,method", MIXED_CASES)
 def test_mixed_methods_reach_target_and_agree(name, method, backend_built, oracle_built):
     g, c, rep, steps = _run(name, method, oracle_built)
     try:
         assert rep["final_rel_residual"] <= REL, rep
         assert rep["fallback_events"] == 0, rep
         assert rep["outer_steps"] >= 2
-        ug, uc = g.read("u"), c.f["u"]
-        hd = g.hd
-        ug = ug.reshape(g.y, g.x)[hd:-hd, hd:-hd]
-        uc = uc.reshape(c.y, c.x)[hd:-hd, hd:-hd]
-        assert np.max(np.abs(ug - uc)) <= 1e-7 * np.max(np.abs(uc))
-        tg, tc = g.summary()[3], c.summary()[3]
-        assert abs(tg - tc) <= 1e-7 * abs(tc)
+        _assert_agree(g, c)
+    finally:
+        g.close()
+
+
+def test_learned_method_refuses_widths_not_divisible_by_4(backend_built, oracle_built):
+    from exploringsycl_gb300 import TLError
+    with pytest.raises(TLError, match="W % 4 == 0"):
+        _run("random_odd_75x90", "mixed-learned", oracle_built)
+
+
+def test_learned_method_agrees_with_oracle_at_1024(backend_built, oracle_built):
+    """The headline solver on a 1024^2 random-state deck (a seed the
+    network was neither trained nor evaluated on), two timesteps: the
+    field summary and u agree with the oracle's FP64 CG."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    from exploringsycl_gb300.learned import Net, load_weights
+    d = dk.random_deck(1024, seed=11, end_step=2)
+    g = GpuChunk(d)
+    c = oracle_built.OracleChunk(d)
+    net = Net(g.ctx, load_weights()[0])
+    try:
+        for _ in range(2):
+            rep = g.solve_timestep("mixed-learned", rel_tol=REL, learned=net)
+            c.cg_timestep(rel_tol=REL)
+            assert rep["final_rel_residual"] <= REL, rep
+        _assert_agree(g, c)
+    finally:
+        net.close()
+        g.close()
+
+
+def test_exhausted_refinement_falls_back_to_fp64_cg(backend_built, oracle_built):
+    """One refinement step cannot reach 1e-10 from an inner solve asked for
+    a 1e-5 reduction: the solve must not stop there but finish with FP64 CG."""
+    g, c, rep, steps = _run("random_160", "mixed", oracle_built, max_outer=1, inner_tol=1e-5)
+    try:
+        assert rep["outer_steps"] == 1
+        assert rep["fallback_events"] == 1
+        assert rep["final_rel_residual"] <= REL
+        _assert_agree(g, c)
     finally:
         g.close()
 
