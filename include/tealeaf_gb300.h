@@ -298,6 +298,8 @@ int tl_solve(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
  * tap = 3*(dy+1) + (dx+1) for input offset (dy, dx). */
 typedef struct tl_net tl_net;
 int tl_net_num_params(void);
+/* A network lives on the context it is created on and uses its stream:
+ * destroy it before that context. */
 int tl_net_create(tl_context* ctx, tl_net** out);
 int tl_net_destroy(tl_net* net);
 int tl_net_set_weights(tl_net* net, const float* host_weights, int n);

@@ -43,6 +43,10 @@ def _run(name, method, oracle_built, deck=None, **kw):
         steps = c.cg_timestep(rel_tol=REL)
         return g, c, rep, steps
     except Exception:
+        # a network belongs to its context: destroy it first
+        if net is not None:
+            net.close()
+            net = None
         g.close()
         raise
     finally:
