@@ -24,9 +24,12 @@
  *    working directory, which remain the defaults);
  *  - a missing tea.problems prints a warning and fails the check instead of
  *    dereferencing a null FILE* (field_summary_driver.c:58-70);
- *  - more than one chunk per rank is rejected with an error: without MPI the
- *    reference exchanges no halos between chunks of one rank
- *    (remote_halo_driver.c:14), so such runs are not meaningful.
+ *  - with more than one chunk (num_chunks_per_rank > 1) the halos between
+ *    the chunks are exchanged: each chunk packs its faces through
+ *    run_pack_or_unpack and the neighbouring chunk unpacks them, in the order
+ *    of remote_halo_driver.c:11-129 (left/right, then bottom/top), where the
+ *    reference built without MPI exchanges nothing (remote_halo_driver.c:14)
+ *    and its chunks would solve uncoupled problems.
  */
 #include <ctype.h>
 #include <float.h>
@@ -481,12 +484,128 @@ void read_config(Settings* settings, State** states) {
 
 /* --------------------------------------------------------------- drivers */
 
+/* TeaLeaf/drivers/remote_halo_driver.c:132-184: packs (or unpacks) every
+ * field marked for exchange into consecutive depth x offset slices of
+ * `buffer`; returns the length used. */
+static int invoke_pack_or_unpack(Chunk* chunk, Settings* settings, int face, int depth,
+                                 int offset, bool pack, double* buffer) {
+  int buffer_len = 0;
+  for (int ii = 0; ii < NUM_FIELDS; ++ii) {
+    if (!settings->fields_to_exchange[ii]) continue;
+    FieldBufferType field;
+    switch (ii) {
+      case FIELD_DENSITY: field = chunk->density; break;
+      case FIELD_ENERGY0: field = chunk->energy0; break;
+      case FIELD_ENERGY1: field = chunk->energy; break;
+      case FIELD_U: field = chunk->u; break;
+      case FIELD_P: field = chunk->p; break;
+      case FIELD_SD: field = chunk->sd; break;
+      default: die(__LINE__, __FILE__, "Incorrect field provided: %d.\n", ii + 1);
+    }
+    double* offset_buffer = buffer + buffer_len;
+    buffer_len += depth * offset;
+    if (settings->kernel_language == C) {
+      run_pack_or_unpack(chunk, settings, depth, face, pack, field, offset_buffer);
+    }
+  }
+  return buffer_len;
+}
+
+/* The exchange of TeaLeaf/drivers/remote_halo_driver.c:11-129 between the
+ * chunks of this rank (one rank: every neighbour is a local chunk, index =
+ * chunk number). A chunk packs each face that has a neighbour into its send
+ * buffer; the neighbour's receive buffer on the opposite face gets a copy,
+ * which stands for the message; then every chunk unpacks. Left/right
+ * first, then bottom/top, whose rows include the halo columns just filled. */
+static void exchange_between_chunks(Chunk* chunks, Settings* settings, int depth) {
+  const int n = settings->num_chunks_per_rank;
+  if (n < 2) return;
+  const int first = settings->rank * n;
+  struct Pair { int face, opposite; };
+  const Pair passes[2][2] = {{{CHUNK_LEFT, CHUNK_RIGHT}, {CHUNK_RIGHT, CHUNK_LEFT}},
+                             {{CHUNK_BOTTOM, CHUNK_TOP}, {CHUNK_TOP, CHUNK_BOTTOM}}};
+  auto send_buffer = [](Chunk* c, int face) {
+    return face == CHUNK_LEFT ? c->left_send : face == CHUNK_RIGHT ? c->right_send
+           : face == CHUNK_BOTTOM ? c->bottom_send : c->top_send;
+  };
+  auto recv_buffer = [](Chunk* c, int face) {
+    return face == CHUNK_LEFT ? c->left_recv : face == CHUNK_RIGHT ? c->right_recv
+           : face == CHUNK_BOTTOM ? c->bottom_recv : c->top_recv;
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int> lens((size_t)n * 2, 0);
+    for (int cc = 0; cc < n; ++cc) {
+      for (int s = 0; s < 2; ++s) {
+        const int face = passes[pass][s].face;
+        if (chunks[cc].neighbours[face] == EXTERNAL_FACE) continue;
+        const int offset = pass == 0 ? chunks[cc].y : chunks[cc].x;
+        lens[(size_t)cc * 2 + s] = invoke_pack_or_unpack(&chunks[cc], settings, face, depth,
+                                                         offset, true,
+                                                         send_buffer(&chunks[cc], face));
+      }
+    }
+    for (int cc = 0; cc < n; ++cc) {
+      for (int s = 0; s < 2; ++s) {
+        const int face = passes[pass][s].face;
+        const int nb = chunks[cc].neighbours[face];
+        if (nb == EXTERNAL_FACE) continue;
+        const int local = nb - first;
+        if (local < 0 || local >= n) {
+          die(__LINE__, __FILE__, "Chunk %d's neighbour %d is not on this rank.\n",
+              first + cc, nb);
+        }
+        /* the neighbour packed its opposite face, slot 1 - s of its pass */
+        const int len = lens[(size_t)local * 2 + (1 - s)];
+        if (len != lens[(size_t)cc * 2 + s]) {
+          die(__LINE__, __FILE__, "Halo lengths of chunks %d and %d differ.\n", first + cc,
+              nb);
+        }
+        memcpy(recv_buffer(&chunks[cc], face),
+               send_buffer(&chunks[local], passes[pass][s].opposite),
+               sizeof(double) * (size_t)len);
+      }
+    }
+    for (int cc = 0; cc < n; ++cc) {
+      for (int s = 0; s < 2; ++s) {
+        const int face = passes[pass][s].face;
+        if (chunks[cc].neighbours[face] == EXTERNAL_FACE) continue;
+        const int offset = pass == 0 ? chunks[cc].y : chunks[cc].x;
+        invoke_pack_or_unpack(&chunks[cc], settings, face, depth, offset, false,
+                              recv_buffer(&chunks[cc], face));
+      }
+    }
+  }
+}
+
 static void halo_update_driver(Chunk* chunks, Settings* settings, int depth) {
-  /* TeaLeaf/drivers/halo_update_driver.c:6-25. With one rank the remote
-   * exchange (remote_halo_driver.c) has nothing to do. */
+  /* TeaLeaf/drivers/halo_update_driver.c:6-25: the exchange between chunks
+   * (remote_halo_driver.c), then the reflective halos of the external
+   * faces. */
   if (!is_fields_to_exchange(settings)) return;
+  exchange_between_chunks(chunks, settings, depth);
   for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
     if (settings->kernel_language == C) run_local_halos(&chunks[cc], settings, depth);
+  }
+}
+
+/* A scalar that the backend overwrites rather than accumulates (r.r of
+ * cg_calc_ur, the 2-norm, the Jacobi error and the field summary:
+ * TeaLeaf/c_kernels/sycl/cg.cpp:253, solver_methods.cpp:116, jacobi.cpp:116,
+ * field_summary.cpp:147-150) holds one chunk's value. With one chunk the
+ * backend writes the driver's variable itself, as in the reference; with
+ * several, the chunks' values are added in chunk order into `total`, which
+ * starts from zero. `call(cc, out)` runs chunk cc's kernel into *out. */
+template <class Call>
+static void sum_chunk_scalars(Settings* settings, double* total, Call call) {
+  if (settings->num_chunks_per_rank == 1) {
+    call(0, total);
+    return;
+  }
+  *total = 0.0;
+  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
+    double v = 0.0;
+    call(cc, &v);
+    *total += v;
   }
 }
 
@@ -515,10 +634,11 @@ static void cg_main_step_driver(Chunk* chunks, Settings* settings, int tt,
   }
   double alpha = *rro / pw;
   double rrn = 0.0;
-  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-    chunks[cc].cg_alphas[tt] = alpha;
-    if (settings->kernel_language == C)
-      run_cg_calc_ur(&chunks[cc], settings, alpha, &rrn);
+  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) chunks[cc].cg_alphas[tt] = alpha;
+  if (settings->kernel_language == C) {
+    sum_chunk_scalars(settings, &rrn, [&](int cc, double* out) {
+      run_cg_calc_ur(&chunks[cc], settings, alpha, out);
+    });
   }
   double beta = rrn / *rro;
   for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
@@ -628,11 +748,11 @@ static void cheby_init_driver(Chunk* chunks, Settings* settings,
   *bb = 0.0;
   eigenvalue_driver_initialise(chunks, settings, num_cg_iters);
   cheby_coef_driver(chunks, settings, settings->max_iters - num_cg_iters);
-  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-    if (settings->kernel_language == C) {
-      run_calculate_2norm(&chunks[cc], settings, chunks[cc].u0, bb);
-      run_cheby_init(&chunks[cc], settings);
-    }
+  if (settings->kernel_language == C) {
+    sum_chunk_scalars(settings, bb, [&](int cc, double* out) {
+      run_calculate_2norm(&chunks[cc], settings, chunks[cc].u0, out);
+    });
+    for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) run_cheby_init(&chunks[cc], settings);
   }
   reset_fields_to_exchange(settings);
   settings->fields_to_exchange[FIELD_U] = true;
@@ -650,9 +770,10 @@ static void cheby_main_step_driver(Chunk* chunks, Settings* settings,
   }
   if (is_calc_2norm) {
     *error = 0.0;
-    for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-      if (settings->kernel_language == C)
-        run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, error);
+    if (settings->kernel_language == C) {
+      sum_chunk_scalars(settings, error, [&](int cc, double* out) {
+        run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, out);
+      });
     }
   }
 }
@@ -742,15 +863,17 @@ static void ppcg_main_step_driver(Chunk* chunks, Settings* settings,
   }
   double alpha = *rro / pw;
   double rrn = 0.0;
-  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-    if (settings->kernel_language == C)
-      run_cg_calc_ur(&chunks[cc], settings, alpha, &rrn);
+  if (settings->kernel_language == C) {
+    sum_chunk_scalars(settings, &rrn, [&](int cc, double* out) {
+      run_cg_calc_ur(&chunks[cc], settings, alpha, out);
+    });
   }
   ppcg_inner_iterations(chunks, settings);
   rrn = 0.0;
-  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-    if (settings->kernel_language == C)
-      run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, &rrn);
+  if (settings->kernel_language == C) {
+    sum_chunk_scalars(settings, &rrn, [&](int cc, double* out) {
+      run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, out);
+    });
   }
   double beta = rrn / *rro;
   for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
@@ -805,16 +928,19 @@ static void jacobi_driver(Chunk* chunks, Settings* settings, double rx,
   settings->fields_to_exchange[FIELD_U] = true;
   int tt;
   for (tt = 0; tt < settings->max_iters; ++tt) {
-    for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-      if (settings->kernel_language == C) run_jacobi_iterate(&chunks[cc], settings, error);
+    if (settings->kernel_language == C) {
+      sum_chunk_scalars(settings, error, [&](int cc, double* out) {
+        run_jacobi_iterate(&chunks[cc], settings, out);
+      });
     }
     if (tt % 50 == 0) {
       halo_update_driver(chunks, settings, 1);
-      for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-        if (settings->kernel_language == C) {
+      if (settings->kernel_language == C) {
+        for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc)
           run_calculate_residual(&chunks[cc], settings);
-          run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, error);
-        }
+        sum_chunk_scalars(settings, error, [&](int cc, double* out) {
+          run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, out);
+        });
       }
     }
     halo_update_driver(chunks, settings, 1);
@@ -829,11 +955,12 @@ static void jacobi_driver(Chunk* chunks, Settings* settings, double rx,
 static void solve_finished_driver(Chunk* chunks, Settings* settings) {
   double exact_error = 0.0;
   if (settings->check_result) {
-    for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-      if (settings->kernel_language == C) {
+    if (settings->kernel_language == C) {
+      for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc)
         run_calculate_residual(&chunks[cc], settings);
-        run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, &exact_error);
-      }
+      sum_chunk_scalars(settings, &exact_error, [&](int cc, double* out) {
+        run_calculate_2norm(&chunks[cc], settings, chunks[cc].r, out);
+      });
     }
   }
   for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
@@ -876,9 +1003,18 @@ static void get_checking_value(Settings* settings, double* checking_value) {
 static void field_summary_driver(Chunk* chunks, Settings* settings,
                                  bool is_solve_finished) {
   double vol = 0.0, ie = 0.0, temp = 0.0, mass = 0.0;
-  for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
-    if (settings->kernel_language == C)
-      run_field_summary(&chunks[cc], settings, &vol, &mass, &ie, &temp);
+  if (settings->kernel_language == C && settings->num_chunks_per_rank == 1) {
+    run_field_summary(&chunks[0], settings, &vol, &mass, &ie, &temp);
+  } else if (settings->kernel_language == C) {
+    /* the sums are overwritten per chunk (see sum_chunk_scalars) */
+    for (int cc = 0; cc < settings->num_chunks_per_rank; ++cc) {
+      double v = 0.0, m = 0.0, e = 0.0, t = 0.0;
+      run_field_summary(&chunks[cc], settings, &v, &m, &e, &t);
+      vol += v;
+      mass += m;
+      ie += e;
+      temp += t;
+    }
   }
   if (settings->rank == MASTER && settings->check_result && is_solve_finished) {
     print_and_log(settings, "\nChecking results...\n");
@@ -953,9 +1089,8 @@ static void decompose_field(Settings* settings, Chunk* chunks) {
 static void initialise_application(Chunk** chunks, Settings* settings) {
   State* states = NULL;
   read_config(settings, &states);
-  if (settings->num_chunks_per_rank != 1) {
-    die(__LINE__, __FILE__,
-        "num_chunks_per_rank=%d: only one chunk per rank is supported.\n",
+  if (settings->num_chunks_per_rank < 1) {
+    die(__LINE__, __FILE__, "num_chunks_per_rank=%d: at least one chunk is needed.\n",
         settings->num_chunks_per_rank);
   }
   if (settings->num_states < 1 || !states[0].defined) {

@@ -348,12 +348,12 @@ def evaluate_loss(net: Net, ds: Dataset, batch: int = 32, crop: int = 128, margi
 
 
 def compare_methods(weights: np.ndarray, size: int, seeds, rel_tol: float = 1e-10,
-                    timestep: float = 0.004) -> dict:
-    """Inner steps and device time of the mixed solves (plain, Jacobi,
-    learned) on fresh random-state problems of the given seeds."""
+                    timestep: float = 0.004,
+                    methods=("mixed", "mixed-jacobi", "mixed-learned")) -> dict:
+    """Inner steps (CG steps for cg64) and device time of the solves on
+    fresh random-state problems of the given seeds, summed over the seeds."""
     from .chunk import GpuChunk
-    out = {m: {"inner_steps": 0, "device_ms": 0.0, "fallbacks": 0}
-           for m in ("mixed", "mixed-jacobi", "mixed-learned")}
+    out = {m: {"inner_steps": 0, "device_ms": 0.0, "fallbacks": 0} for m in methods}
     for seed in seeds:
         d = dk.random_deck(size, seed=seed, end_step=1, initial_timestep=timestep)
         for method in out:
@@ -450,5 +450,38 @@ def train_cli(argv=None) -> None:
     ctx.close()
 
 
+def evaluate_cli(argv=None) -> None:
+    """python -m exploringsycl_gb300.learned evaluate [--sizes 1024,4096] ...
+
+    Solves one timestep of fresh random-state problems (seeds the network
+    was neither trained nor tuned on) to the relative FP64 true residual
+    1e-10 with plain FP64 CG (cg64), the FP32-inner CG and Jacobi-PCG in FP64
+    refinement, and the learned PCG in FP64 refinement; prints, per size and
+    per seed, each method's steps, device time, fall-backs and final
+    residual as one JSON line."""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
+    ap.add_argument("--sizes", default="1024,4096")
+    ap.add_argument("--seeds", default="31,32,33")
+    ap.add_argument("--seeds-large", default="31",
+                    help="seeds for sizes above 2048 (each plain FP64 CG solve takes seconds)")
+    args = ap.parse_args(argv)
+    w, meta = load_weights(args.weights)
+    methods = ("cg64", "mixed", "mixed-jacobi", "mixed-learned")
+    result = {"weights": str(args.weights), "rel_tol": 1e-10, "timestep": 0.004,
+              "training": {k: meta.get(k) for k in ("data", "like", "seed0", "steps")},
+              "sizes": {}}
+    for size in (int(v) for v in args.sizes.split(",")):
+        seeds = [int(v) for v in (args.seeds_large if size > 2048 else args.seeds).split(",")]
+        per_seed = {seed: compare_methods(w, size, [seed], methods=methods) for seed in seeds}
+        result["sizes"][size] = {"seeds": seeds, "per_seed": per_seed}
+    print(json.dumps(result))
+
+
 if __name__ == "__main__":
-    train_cli()
+    import sys
+    if len(sys.argv) > 1 and sys.argv[1] == "evaluate":
+        evaluate_cli(sys.argv[2:])
+    else:
+        train_cli()

@@ -191,3 +191,20 @@ def test_solve_that_ends_above_its_target_stops_the_run(fake_driver, tmp_path):
     assert "above the target 1.000e-10" in r.stdout
     assert "tl_field_summary" not in _names(calls[calls.index(
         next(c for c in calls if c.startswith("tl_solve"))):])
+
+
+def test_several_chunks_use_the_step_wise_kernels(fake_driver, tmp_path):
+    """With more than one chunk the chunks' CG solves are coupled through the
+    driver's sums, so the backend gives up its run-ahead device solve and
+    refuses a whole-timestep replacement solver."""
+    d = dk.two_state(16, end_step=1, max_iters=3)
+    d.extra = ["num_chunks_per_rank 2"]
+    r, calls = _run(fake_driver, d, tmp_path / "a")
+    assert r.returncode == 0, r.stdout[-1500:]
+    names = _names(calls)
+    assert "tl_cg_solve" not in names and "tl_cg_calc_w" in names
+    assert "tl_pack_or_unpack" in names
+    d.extra = ["num_chunks_per_rank 2", "gb300_solver mixed"]
+    r, calls = _run(fake_driver, d, tmp_path / "b")
+    assert r.returncode == 1
+    assert "solve one chunk; this run has 2 chunks per rank" in r.stdout

@@ -39,6 +39,40 @@ def test_driver_matches_oracle(name, mode, tmp_path, backend_built, oracle_built
     assert gpu.summaries == cpu.summaries and gpu.summaries
 
 
+def _chunked(make, chunks):
+    def deck():
+        d = make()
+        d.extra = [f"num_chunks_per_rank {chunks}"]
+        return d
+    return deck
+
+
+MULTI_CHUNK = {
+    "cg_64_4chunks": _chunked(lambda: dk.five_state(64, end_step=2), 4),
+    "random_80_3chunks": _chunked(lambda: dk.random_deck(80, seed=11, end_step=2), 3),
+    "two_state_130x70_6chunks": _chunked(
+        lambda: dk.Deck(130, 70, dk.two_state(1).states, end_step=2), 6),
+    "jacobi_40_2chunks": _chunked(
+        lambda: dk.five_state(40, end_step=2, max_iters=400, solver="jacobi"), 2),
+    "ppcg_64_4chunks": _chunked(
+        lambda: dk.five_state(64, end_step=2, solver="ppcg", presteps=8), 4),
+}
+
+
+@pytest.mark.parametrize("name", list(MULTI_CHUNK))
+def test_several_chunks_match_oracle(name, tmp_path, backend_built, oracle_built):
+    """Several chunks on one rank: the chunks exchange halos through
+    run_pack_or_unpack and the driver sums their scalars in chunk order, the
+    same on both backends, so the output is identical bit for bit."""
+    d = MULTI_CHUNK[name]()
+    gpu = run_driver(DRIVER_EXE, d, tmp_path / "gpu")
+    cpu = run_driver(oracle_built.DRIVER, d, tmp_path / "cpu")
+    assert gpu.returncode == 0, gpu.stdout[-2000:]
+    assert cpu.returncode == 0, cpu.stdout[-2000:]
+    assert gpu.comparable() == cpu.comparable()
+    assert gpu.summaries == cpu.summaries and gpu.summaries
+
+
 @pytest.mark.parametrize("n,steps", [(10, 10), (64, 1), (250, 10)])
 def test_tabulated_temperature(n, steps, tmp_path, backend_built):
     run = run_driver(DRIVER_EXE, dk.five_state(n, end_step=steps), tmp_path)
