@@ -72,6 +72,24 @@ INNER_BYTES = {"mixed": 48, "mixed-jacobi": 56}
 # z, p_old, kx, ky, e and writes p_new, w, e (32 B); phase Z reads r, w, s and
 # writes r, z (20 B).
 LEARNED_BYTES = 52
+
+
+def coarse_unknowns(size: int) -> int:
+    """Coarse unknowns of the two-level learned PCG on a size^2 grid: the
+    smallest aggregate of 32, 64, 128 cells that divides the side and leaves
+    at most 4096 (tl_coarse.cu)."""
+    for blk in (32, 64, 128):
+        if size % blk == 0 and (size // blk) ** 2 <= 4096:
+            return (size // blk) ** 2
+    return 0
+
+
+def learned_bytes(solver: str, size: int) -> float:
+    """Algorithmic bytes per cell and inner step; the two-level step also
+    reads the FP32 inverse of the coarse operator once (4 nc^2 bytes)."""
+    if solver == "mixed-learned-coarse":
+        return LEARNED_BYTES + 4.0 * coarse_unknowns(size) ** 2 / (size * size)
+    return LEARNED_BYTES
 # FP64 operations per cell of one CG step: exact contract (stencil 9 with the
 # precomputed diagonal, dot products 2 x 1.6, u/r update 4, p update 2) and fused
 # multiply-add contract (stencil 5, dot products 2 x 1.6, u/r 2, p 1). Of these,
@@ -178,6 +196,9 @@ def config_for(args, steps_per_timestep=None) -> dict:
               "mixed-learned": "FP32 inner PCG with the learned preconditioner "
                                "(network collapsed to a 17x17 stencil on the tensor cores) "
                                "in FP64 iterative refinement",
+              "mixed-learned-coarse": "FP32 inner PCG with the learned preconditioner plus "
+                                      "a coarse level (aggregates, dense FP32 inverse of "
+                                      "P^T A P) in FP64 iterative refinement",
               }[args.solver]
     return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "
                         f"{stop_rule(args.solver)}, consecutive timesteps",
@@ -282,7 +303,7 @@ class Stepper:
         self.max_inner = args.max_inner
         self.max_outer = args.max_outer
         self.net = None
-        if solver == "mixed-learned":
+        if solver.startswith("mixed-learned"):
             from exploringsycl_gb300.learned import Net, load_weights
             w, _ = load_weights()
             self.net = Net(ctx, w)
@@ -412,7 +433,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
                                     "oracle), same stop rule"),
                   ("cg64", "fused", "plain FP64 CG (fused multiply-add contract), "
                                     "same stop rule")]
-        for solver in ("mixed-jacobi", "mixed-learned"):
+        for solver in ("mixed-jacobi", "mixed-learned", "mixed-learned-coarse"):
             if solver != args.solver:
                 others.append((solver, args.fp64, f"{solver}, same stop rule"))
         for solver, contract, label in others:
@@ -444,14 +465,14 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     peaks = load_peaks()
     if args.solver in ("plain", "cg64"):
         kernel, bpc = "cg_persistent_kernel", BYTES_PER_CELL_STEP
-    elif args.solver == "mixed-learned":
-        kernel, bpc = "lpcg_kernel", LEARNED_BYTES
+    elif args.solver.startswith("mixed-learned"):
+        kernel, bpc = "lpcg_kernel", learned_bytes(args.solver, args.size)
     else:
         kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
     achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9
     traffic = None
     key = (kernel, args.fp64 if kernel == "cg_persistent_kernel" else None)
-    if NCU_BYTES_PER_CELL_STEP.get(key) is not None:
+    if args.solver != "mixed-learned-coarse" and NCU_BYTES_PER_CELL_STEP.get(key) is not None:
         # ncu DRAM bytes per cell and step x the cells and steps of one timestep
         traffic = NCU_BYTES_PER_CELL_STEP[key] * cells * k_steps
     roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -539,7 +560,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--deck", choices=["random", "two-state"], default="random")
-    ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned", "cg64", "plain"],
+    ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned",
+                                         "mixed-learned-coarse", "cg64", "plain"],
                     default="mixed-learned")
     ap.add_argument("--fp64", choices=["exact", "fused"], default="exact",
                     help="arithmetic contract of the persistent FP64 CG (plain, cg64, fall-back)")

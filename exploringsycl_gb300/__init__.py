@@ -56,10 +56,12 @@ class TLSolveReport(C.Structure):
 
 METHOD_CG64, METHOD_MIXED_CG, METHOD_MIXED_JACOBI, METHOD_MIXED_LEARNED = 0, 1, 2, 3
 METHOD_MIXED_LEARNED_LAYERS = 4
+METHOD_MIXED_LEARNED_COARSE = 5
 FP64_CONTRACTS = {"exact": 0, "fused": 1}
 METHODS = {"cg64": METHOD_CG64, "mixed": METHOD_MIXED_CG, "mixed-jacobi": METHOD_MIXED_JACOBI,
            "mixed-learned": METHOD_MIXED_LEARNED,
-           "mixed-learned-layers": METHOD_MIXED_LEARNED_LAYERS}
+           "mixed-learned-layers": METHOD_MIXED_LEARNED_LAYERS,
+           "mixed-learned-coarse": METHOD_MIXED_LEARNED_COARSE}
 
 
 class TLState(C.Structure):
@@ -136,6 +138,7 @@ HANDLE_FIRST = {
     "tl_net_gather_crops": [_P, _I, _I, C.POINTER(C.c_int), _I, _I, _I, _P],
     "tl_pack_interior": [_I, _I, _I, _P, _D, _P],
     "tl_pack_coefficients": [_I, _I, _I, _P, _P, _P, _P, _P],
+    "tl_coarse_inverse": [_I, _I, _P, _P, _PI, _PI, C.POINTER(C.c_float), C.c_size_t],
 }
 
 _lib = None

@@ -34,7 +34,7 @@
  * fails.
  *
  * Solver replacement. With the deck key `gb300_solver <cg64|mixed|
- * mixed-jacobi|mixed-learned>` (or TL_SOLVER in the environment;
+ * mixed-jacobi|mixed-learned|mixed-learned-coarse>` (or TL_SOLVER in the environment;
  * `preconditioner_on` alone selects mixed-jacobi; mixed-learned reads the
  * network's weights from `gb300_weights <file>` or TL_WEIGHTS: raw
  * little-endian FP32, tl_net_num_params() values), run_cg_init solves the timestep with
@@ -91,6 +91,7 @@ static int method_from_name(const char* name) {
   if (strcmp(name, "mixed") == 0) return TL_METHOD_MIXED_CG;
   if (strcmp(name, "mixed-jacobi") == 0) return TL_METHOD_MIXED_JACOBI;
   if (strcmp(name, "mixed-learned") == 0) return TL_METHOD_MIXED_LEARNED;
+  if (strcmp(name, "mixed-learned-coarse") == 0) return TL_METHOD_MIXED_LEARNED_COARSE;
   if (strcmp(name, "cg") == 0 || strcmp(name, "reference") == 0) return -1;
   die(__LINE__, __FILE__, "GB300 backend: unknown solver '%s'\n", name);
   return -1;
@@ -153,7 +154,9 @@ static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
   if (env) snprintf(weights, sizeof(weights), "%s", env);
   TL_TRY(tl_set_fp64_contract(ext->ctx, ext->fp64_fused ? TL_FP64_FUSED : TL_FP64_EXACT),
          "FP64 contract");
-  if (ext->replace_method == TL_METHOD_MIXED_LEARNED) load_network(ext, weights);
+  if (ext->replace_method == TL_METHOD_MIXED_LEARNED ||
+      ext->replace_method == TL_METHOD_MIXED_LEARNED_COARSE)
+    load_network(ext, weights);
 }
 
 /* TeaLeaf/c_kernels/sycl/kernel_initialise.cpp:31-80 */

@@ -89,6 +89,10 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_stage);
   cudaFree(ctx->d_diag);
   cudaFree(ctx->d_f32);
+  cudaFree(ctx->d_ainv);
+  cudaFree(ctx->d_coarse_work);
+  cudaFree(ctx->d_coarse_vec);
+  cudaFree(ctx->d_hash);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
   if (ctx->h_steps) cudaFreeHost(ctx->h_steps);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);

@@ -83,6 +83,29 @@ struct tl_context {
   cudaEvent_t ev_stop = nullptr;
   tl_solve_stats last_solve = {0.0f, 0, 0};
   int fp64_fused = 0;             /* TL_FP64_FUSED: the persistent FP64 CG uses FMAs */
+  /* coarse level of the two-level learned PCG (tl_coarse.cu): the FP32
+   * inverse of the coarse operator of the couplings last seen, kept while
+   * they do not change, and its per-step vectors */
+  float* d_ainv = nullptr;        /* nc x nc, row-major */
+  size_t ainv_cap = 0;
+  double* d_coarse_work = nullptr; /* the inverse's FP64 columns, then the bands */
+  size_t coarse_work_cap = 0;
+  float* d_coarse_vec = nullptr;  /* tile restriction partials, then e_c */
+  size_t coarse_vec_cap = 0;
+  unsigned long long* d_hash = nullptr;
+  int coarse_H = 0, coarse_W = 0, coarse_blk = 0;
+  unsigned long long coarse_hash = 0;
+};
+
+/* The coarse level of a packed [H][W] field: blk x blk aggregates
+ * (blk = 1 << blk_shift), an ncx x ncy coarse grid of nc unknowns, the
+ * inverse of its operator P^T A P (FP32, row-major nc x nc), the per-tile
+ * restriction partials (8 per 128 x 64 tile) and the coarse correction e_c. */
+struct tl_coarse_level {
+  int blk_shift, ncx, ncy, nc;
+  const float* ainv;
+  float* rc_part;
+  float* ec;
 };
 
 /* Thread-local error message and helpers (tl_context.cu). */
@@ -116,7 +139,11 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
                                int W, const float* kx, const float* ky, const float* s,
                                float* r, float* r_alt, float* e, float* w, float* z, float* pa,
                                float* pb, double tol, int max_iters, int* iters,
-                               double* rr_final);
+                               double* rr_final, const tl_coarse_level* coarse = nullptr);
+/* The coarse level for the couplings kx, ky of a packed [H][W] field
+ * (tl_coarse.cu): rebuilt only when H, W or the couplings change. */
+int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, const float* ky,
+                               tl_coarse_level* out);
 int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
                                   int max_iters, double* p, double* r, double* u,
                                   const double* u0, double* w, const double* kx,

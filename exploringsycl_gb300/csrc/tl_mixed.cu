@@ -453,10 +453,12 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
   } else {
     TL_REQUIRE(prm->method == TL_METHOD_MIXED_CG || prm->method == TL_METHOD_MIXED_JACOBI ||
                    prm->method == TL_METHOD_MIXED_LEARNED ||
-                   prm->method == TL_METHOD_MIXED_LEARNED_LAYERS,
+                   prm->method == TL_METHOD_MIXED_LEARNED_LAYERS ||
+                   prm->method == TL_METHOD_MIXED_LEARNED_COARSE,
                "tl_solve: unknown method");
     const bool layers = prm->method == TL_METHOD_MIXED_LEARNED_LAYERS;
-    const bool learned = layers || prm->method == TL_METHOD_MIXED_LEARNED;
+    const bool two_level = prm->method == TL_METHOD_MIXED_LEARNED_COARSE;
+    const bool learned = layers || two_level || prm->method == TL_METHOD_MIXED_LEARNED;
     const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : (learned ? 3e-6 : 1e-5);
     TL_REQUIRE(!learned || prm->learned, "tl_solve: the learned method needs a network");
     const int H = y - 2 * hd, W = x - 2 * hd;
@@ -474,10 +476,16 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     float *kx32 = f, *ky32 = f + cap, *invd = f + 2 * cap, *r32 = f + 3 * cap,
           *e32 = f + 4 * cap, *w32 = f + 5 * cap, *pa = f + 6 * cap, *pb = f + 7 * cap,
           *z32 = f + 8 * cap, *r32b = f + 9 * cap;
+    tl_coarse_level coarse;
     if (learned) {
       /* packed layout: kx32, ky32, invd hold the packed kx, ky, s */
       rc = tl_pack_coefficients(ctx, x, y, hd, kx, ky, kx32, ky32, invd);
       if (rc != TL_OK) return rc;
+      if (two_level) {
+        /* the coarse level of this operator (rebuilt only when it changes) */
+        rc = tl_internal_coarse_prepare(ctx, H, W, kx32, ky32, &coarse);
+        if (rc != TL_OK) return rc;
+      }
     } else {
       coeff_kernel<<<grid_for(ctx, len), 256, 0, ctx->stream>>>(x, y, hd, kx, ky, kx32, ky32,
                                                                 invd);
@@ -541,7 +549,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
           if (rc != TL_OK) return rc;
           rc = tl_internal_fpcg_collapsed(ctx, umma, kscale, H, W, kx32, ky32, invd, r32, r32b,
                                           e32, w32, z32, pa, pb, tol, prm->max_inner, &it,
-                                          &rr_in);
+                                          &rr_in, two_level ? &coarse : nullptr);
         }
         if (rc != TL_OK) return rc;
         TL_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));

@@ -106,9 +106,16 @@ constexpr int kOffZ = kOffB + kBBytes;
 constexpr int kOffBar = kOffZ + kTH * kZStride * 4;
 constexpr int kOffTmem = kOffBar + (5 + 2 * kIssuers) * 8;
 constexpr int kLpcgSmem = (kOffTmem + 8 + 127) / 128 * 128;
+/* two-level kernel: the epilogue's restriction sums of the tile row pairs
+ * (two tiles in flight x 64 pairs x 2 aggregate columns), then r_c and e_c */
+constexpr int kMaxCoarse = 4096;
+constexpr int kRestSlots = 8;           /* restriction partials per tile */
+constexpr int kOffRest = kLpcgSmem;
+constexpr int kOffCoarse = kOffRest + 2 * (kTH / 2) * 2 * 4;
+constexpr int kLpcgSmemCoarse = kOffCoarse + 2 * kMaxCoarse * 4;
 static_assert(kOffB % 128 == 0 && kOffZ % 16 == 0 && kOffBar % 8 == 0,
               "alignment");
-static_assert(kLpcgSmem <= 227 * 1024, "shared memory");
+static_assert(kLpcgSmemCoarse <= 227 * 1024, "shared memory");
 static_assert(2 * kDCols <= kTmemCols, "tensor memory");
 
 struct LpcgParams {
@@ -120,6 +127,13 @@ struct LpcgParams {
   const __half* umma;  /* window B operands, 17 x 32 x 16 FP16 */
   const float* kscale;
   double* part;  /* 3 arrays of gridDim.x partial sums: p.w, r.r, r.z */
+  /* coarse level (two-level kernel only): blk = 1 << cshift aggregates on an
+   * ncx-wide coarse grid of nc unknowns, Ac^-1 (FP32, nc x nc), the tiles'
+   * restriction partials (8 per tile) and the correction e_c */
+  int cshift, ncx, nc;
+  const float* ainv;
+  float* rc_part;
+  float* ec;
   unsigned* sync;
   int* status;
   int* iters_out;
@@ -177,9 +191,15 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
 /* ------------------------------------------------------------ phase P */
 
 /* p_new = z + beta p_old, w = A p_new, p.w; and the previous step's
- * e += alpha_prev p_old (p_old is loaded here anyway). */
+ * e += alpha_prev p_old (p_old is loaded here anyway). Two-level kernel
+ * (kCoarse): z is the learned part in memory plus the coarse correction of
+ * the cell's aggregate, e_c[(y >> cshift) * ncx + (x >> cshift)] from s_ec
+ * (aggregates are at least 32 wide, so the four cells of a thread share
+ * one). */
+template <bool kCoarse>
 __device__ __forceinline__ float phase_p(const LpcgParams& P, const float* __restrict__ pold,
-                                         float* __restrict__ pnew, float bf, float a_prev) {
+                                         float* __restrict__ pnew, float bf, float a_prev,
+                                         const float* __restrict__ s_ec) {
   const int H = P.H, W = P.W;
   const size_t n = (size_t)H * W;
   const int lane = threadIdx.x & 31;
@@ -192,19 +212,38 @@ __device__ __forceinline__ float phase_p(const LpcgParams& P, const float* __res
     const int xx0 = act ? (int)(i0 - (size_t)yy * W) : 0;
     float4 pc = make_float4(0.f, 0.f, 0.f, 0.f), pu = pc, pd = pc, kxc = pc, kyc = pc,
            kyu = pc;
+    auto coarse_at = [&](int y, int x) -> float {
+      if constexpr (kCoarse) return s_ec[(y >> P.cshift) * P.ncx + (x >> P.cshift)];
+      return 0.0f;
+    };
     if (act) {
-      const float4 zc = ld4(z + i0), oc = ld4(pold + i0);
+      float4 zc = ld4(z + i0);
+      const float4 oc = ld4(pold + i0);
+      if constexpr (kCoarse) {
+        const float c = coarse_at(yy, xx0);
+        zc.x += c; zc.y += c; zc.z += c; zc.w += c;
+      }
       float4 ev = ld4(P.e + i0);
       pc = make_float4(zc.x + bf * oc.x, zc.y + bf * oc.y, zc.z + bf * oc.z, zc.w + bf * oc.w);
       ev.x += a_prev * oc.x; ev.y += a_prev * oc.y; ev.z += a_prev * oc.z; ev.w += a_prev * oc.w;
       *reinterpret_cast<float4*>(P.e + i0) = ev;
       if (yy + 1 < H) {
-        const float4 zu = ld4(z + i0 + W), ou = ld4(pold + i0 + W);
+        float4 zu = ld4(z + i0 + W);
+        const float4 ou = ld4(pold + i0 + W);
+        if constexpr (kCoarse) {
+          const float c = coarse_at(yy + 1, xx0);
+          zu.x += c; zu.y += c; zu.z += c; zu.w += c;
+        }
         pu = make_float4(zu.x + bf * ou.x, zu.y + bf * ou.y, zu.z + bf * ou.z, zu.w + bf * ou.w);
         kyu = __ldg(reinterpret_cast<const float4*>(P.ky + i0 + W));
       }
       if (yy > 0) {
-        const float4 zd = ld4(z + i0 - W), od = ld4(pold + i0 - W);
+        float4 zd = ld4(z + i0 - W);
+        const float4 od = ld4(pold + i0 - W);
+        if constexpr (kCoarse) {
+          const float c = coarse_at(yy - 1, xx0);
+          zd.x += c; zd.y += c; zd.z += c; zd.w += c;
+        }
         pd = make_float4(zd.x + bf * od.x, zd.y + bf * od.y, zd.z + bf * od.z, zd.w + bf * od.w);
       }
       kxc = __ldg(reinterpret_cast<const float4*>(P.kx + i0));
@@ -213,9 +252,15 @@ __device__ __forceinline__ float phase_p(const LpcgParams& P, const float* __res
     float pl = __shfl_up_sync(TL_FULL_MASK, pc.w, 1);
     float pr = __shfl_down_sync(TL_FULL_MASK, pc.x, 1);
     float kx4 = __shfl_down_sync(TL_FULL_MASK, kxc.x, 1);
-    if (lane == 0 && act && xx0 > 0) pl = __ldcg(z + i0 - 1) + bf * __ldcg(pold + i0 - 1);
+    if (lane == 0 && act && xx0 > 0) {
+      float zl = __ldcg(z + i0 - 1);
+      if constexpr (kCoarse) zl += coarse_at(yy, xx0 - 1);
+      pl = zl + bf * __ldcg(pold + i0 - 1);
+    }
     if (lane == 31 && act && xx0 + 4 < W) {
-      pr = __ldcg(z + i0 + 4) + bf * __ldcg(pold + i0 + 4);
+      float zr = __ldcg(z + i0 + 4);
+      if constexpr (kCoarse) zr += coarse_at(yy, xx0 + 4);
+      pr = zr + bf * __ldcg(pold + i0 + 4);
       kx4 = __ldg(P.kx + i0 + 4);
     }
     if (!act) continue;
@@ -258,6 +303,11 @@ struct ZArgs {
   const float* s;
   float* z;
   float alpha, sigma, zscale;
+  /* two-level kernel: the row-pair sums of the tiles in flight
+   * (rest[parity][pair][aggregate column]) and the tiles' partials */
+  float* rest;
+  float* rc_part;
+  int cshift;
 };
 
 /* Per-block tcgen05 state. The phase parities are kept by the threads that
@@ -399,6 +449,7 @@ __device__ __forceinline__ void z_issuer_warp(const ZArgs& A, TileState& T, int*
  * tile zt, then every worker forms z = s K y / sigma + s^2 r_new for its cells
  * from zt, r_new (written by the staging, read back from L2) and s, with
  * coalesced accesses, and sums r.r and r.z. */
+template <bool kCoarse>
 __device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSums& sums,
                                               int* status, int tile, int bb) {
   const int tid = threadIdx.x - 32 * kIssuers;
@@ -439,19 +490,54 @@ __device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSum
   for (int q = tid; q < kQuads; q += kWorkers) {
     const int row = q / (kTW / 4), c4 = 4 * (q % (kTW / 4));
     const int gy = y0 + row, gx = x0 + c4;
-    if (gy >= A.H || gx >= A.W) continue;
-    const size_t i = (size_t)gy * A.W + gx;
-    const float4 rn = ld4(A.rnew + i);
-    const float4 ss = __ldg(reinterpret_cast<const float4*>(A.s + i));
-    const float4 acc = *reinterpret_cast<const float4*>(zt + row * kZStride + c4);
-    float4 zv;
-    zv.x = ss.x * (acc.x * A.zscale) + ss.x * ss.x * rn.x;
-    zv.y = ss.y * (acc.y * A.zscale) + ss.y * ss.y * rn.y;
-    zv.z = ss.z * (acc.z * A.zscale) + ss.z * ss.z * rn.z;
-    zv.w = ss.w * (acc.w * A.zscale) + ss.w * ss.w * rn.w;
-    *reinterpret_cast<float4*>(A.z + i) = zv;
-    sums.rr += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
-    sums.rz += rn.x * zv.x + rn.y * zv.y + rn.z * zv.z + rn.w * zv.w;
+    float rsum = 0.0f;
+    if (gy < A.H && gx < A.W) {
+      const size_t i = (size_t)gy * A.W + gx;
+      const float4 rn = ld4(A.rnew + i);
+      const float4 ss = __ldg(reinterpret_cast<const float4*>(A.s + i));
+      const float4 acc = *reinterpret_cast<const float4*>(zt + row * kZStride + c4);
+      float4 zv;
+      zv.x = ss.x * (acc.x * A.zscale) + ss.x * ss.x * rn.x;
+      zv.y = ss.y * (acc.y * A.zscale) + ss.y * ss.y * rn.y;
+      zv.z = ss.z * (acc.z * A.zscale) + ss.z * ss.z * rn.z;
+      zv.w = ss.w * (acc.w * A.zscale) + ss.w * ss.w * rn.w;
+      *reinterpret_cast<float4*>(A.z + i) = zv;
+      sums.rr += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
+      sums.rz += rn.x * zv.x + rn.y * zv.y + rn.z * zv.z + rn.w * zv.w;
+      if constexpr (kCoarse) rsum = (rn.x + rn.y) + (rn.z + rn.w);
+    }
+    if constexpr (kCoarse) {
+      /* The restriction: a warp holds the 32 quads of tile rows 2m and 2m+1
+       * (16 per row); sum them per aggregate column (8-lane groups for
+       * 32-wide aggregates, whole rows otherwise), then the two rows. */
+      rsum += __shfl_xor_sync(TL_FULL_MASK, rsum, 1);
+      rsum += __shfl_xor_sync(TL_FULL_MASK, rsum, 2);
+      rsum += __shfl_xor_sync(TL_FULL_MASK, rsum, 4);
+      if (A.cshift > 5) rsum += __shfl_xor_sync(TL_FULL_MASK, rsum, 8);
+      rsum += __shfl_xor_sync(TL_FULL_MASK, rsum, 16);
+      float* rest = A.rest + bb * kTH + (q >> 5) * 2;  /* [parity][pair][column] */
+      if (lane == 0) rest[0] = rsum;
+      if (lane == 8 && A.cshift == 5) rest[1] = rsum;
+    }
+  }
+}
+
+/* One worker warp, after a worker barrier that follows z_finish_tile of
+ * `tile` (processing parity bb): the tile's restriction partials, the sums
+ * of its row-pair sums over each aggregate in a fixed order, into
+ * rc_part[tile * kRestSlots + local aggregate] (aggregate rows of the tile
+ * first, then columns). */
+__device__ __forceinline__ void z_restrict_tile(const ZArgs& A, int tile, int bb) {
+  const int lane = threadIdx.x & 31;
+  const int b = 1 << A.cshift;
+  const int arows = b < kTH ? b : kTH, acols = b < kTW ? b : kTW;
+  const int ncol = kTW / acols, nloc = (kTH / arows) * ncol;
+  if (lane < nloc) {
+    const int ar = lane / ncol, ac = lane - ar * ncol;
+    const float* rest = A.rest + bb * kTH;
+    float t = 0.0f;
+    for (int m = ar * arows / 2; m < (ar + 1) * arows / 2; ++m) t += rest[m * 2 + ac];
+    A.rc_part[(size_t)tile * kRestSlots + lane] = t;
   }
 }
 
@@ -459,10 +545,12 @@ __device__ __forceinline__ void z_finish_tile(const ZArgs& A, TileState& T, ZSum
  * for its own cells), then finish tile j - 1. The hand-over tile is
  * single-buffered: a worker barrier separates the last reads of one tile's
  * rows from the readers' writes of the next. */
+template <bool kCoarse>
 __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSums& sums,
                                                int* status) {
   const int tid = threadIdx.x - 32 * kIssuers;
   int prev = -1, prev_b = 0, j = 0;
+  int pend = -1, pend_b = 0;  /* a finished tile whose restriction is still to be summed */
   for (int c = blockIdx.x; c < A.tiles; c += gridDim.x, ++j) {
     const int tile = A.tiles - 1 - c;
     const int b = j & 1;
@@ -471,7 +559,15 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
     tc05::fence_proxy_async_smem();
     named_sync(kBarWorkers, kWorkers);
     if (tid == 0) mbar_arrive(&T.a_full[b]);
-    if (prev >= 0) z_finish_tile(A, T, sums, status, prev, prev_b);
+    if constexpr (kCoarse) {
+      if (pend >= 0 && tid < 32) z_restrict_tile(A, pend, pend_b);
+      pend = -1;
+    }
+    if (prev >= 0) {
+      z_finish_tile<kCoarse>(A, T, sums, status, prev, prev_b);
+      pend = prev;
+      pend_b = prev_b;
+    }
     prev = tile;
     prev_b = b;
   }
@@ -480,19 +576,90 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
    * loop the barrier after staging does this). */
   if (prev >= 0) {
     named_sync(kBarWorkers, kWorkers);
-    z_finish_tile(A, T, sums, status, prev, prev_b);
+    if constexpr (kCoarse) {
+      if (pend >= 0 && tid < 32) z_restrict_tile(A, pend, pend_b);
+    }
+    z_finish_tile<kCoarse>(A, T, sums, status, prev, prev_b);
+    if constexpr (kCoarse) {
+      named_sync(kBarWorkers, kWorkers);
+      if (tid < 32) z_restrict_tile(A, prev, prev_b);
+    }
   }
 }
 
 /* ------------------------------------------------------ persistent PCG */
 
+/* ------------------------------------------------------------ phase C */
+
+/* Two-level kernel, after phase Z's grid barrier: r_c = P^T r_new from the
+ * tiles' restriction partials into s_rc (every block assembles the whole
+ * vector, in the same order), then this block's share of the rows of
+ * e_c = Ac^-1 r_c into P.ec, one warp per row, FP32 sums in a fixed order. */
+__device__ __forceinline__ void phase_c_gemv(const LpcgParams& P, float* s_rc) {
+  const int b = 1 << P.cshift;
+  const int arows = b < kTH ? b : kTH, acols = b < kTW ? b : kTW;
+  const int ncol = kTW / acols;
+  for (int I = threadIdx.x; I < P.nc; I += blockDim.x) {
+    const int Jc = I / P.ncx, Ic = I - Jc * P.ncx;
+    const int gy = Jc << P.cshift, gx = Ic << P.cshift;
+    const int tile = (gy / kTH) * P.tiles_x + gx / kTW;
+    const int loc = ((gy % kTH) / arows) * ncol + (gx % kTW) / acols;
+    float v = __ldcg(P.rc_part + (size_t)tile * kRestSlots + loc);
+    if (b > kTW) v += __ldcg(P.rc_part + (size_t)(tile + 1) * kRestSlots);
+    s_rc[I] = v;
+  }
+  __syncthreads();
+  const int rows = (P.nc + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int r0 = blockIdx.x * rows, r1 = min(P.nc, r0 + rows);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int I = r0 + warp; I < r1; I += (int)(blockDim.x >> 5)) {
+    const float* row = P.ainv + (size_t)I * P.nc;
+    float acc = 0.0f;
+    if ((P.nc & 3) == 0) {
+      const float4* row4 = reinterpret_cast<const float4*>(row);
+      const float4* rc4 = reinterpret_cast<const float4*>(s_rc);
+      for (int q = lane; q < (P.nc >> 2); q += 32) {
+        const float4 a = __ldg(row4 + q);
+        const float4 r = rc4[q];
+        acc += a.x * r.x + a.y * r.y + a.z * r.z + a.w * r.w;
+      }
+    } else {
+      for (int q = lane; q < P.nc; q += 32) acc += __ldg(row + q) * s_rc[q];
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) P.ec[I] = acc;
+  }
+}
+
+/* r_c . e_c in double, in one fixed order, the same in every block. */
+__device__ __forceinline__ double coarse_dot(const float* s_rc, const float* s_ec, int nc,
+                                             double* s_one) {
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nc; i += 32) v += (double)s_rc[i] * (double)s_ec[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TL_FULL_MASK, v, o);
+    if (threadIdx.x == 0) *s_one = v;
+  }
+  __syncthreads();
+  const double t = *s_one;
+  __syncthreads();
+  return t;
+}
+
 /* The solve; returns when done or when a wait ran out (status set). */
+template <bool kCoarse>
 __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, float* s_red,
                                           double* s_one) {
   const int G = gridDim.x;
   const int H = P.H, W = P.W;
   const double n = (double)H * (double)W;
   const float zscale_k = 1.0f / __ldg(P.kscale);
+  /* two-level kernel only (the one-level kernel's shared memory ends
+   * before these regions and never touches them) */
+  float* s_rest = reinterpret_cast<float*>(T.smem + kOffRest);
+  float* s_rc = reinterpret_cast<float*>(T.smem + kOffCoarse);
+  float* s_ec = s_rc + kMaxCoarse;
   double* part_pw = P.part;
   double* part_rr = P.part + G;
   double* part_rz = P.part + 2 * G;
@@ -523,7 +690,7 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     float* pnew = par_p ? P.p0 : P.p1;
     if (k > 0) {
       /* ---- phase P */
-      float pw = phase_p(P, pold, pnew, (float)beta, (float)alpha);
+      float pw = phase_p<kCoarse>(P, pold, pnew, (float)beta, (float)alpha, s_ec);
       pw = block_sum(pw, s_red);
       if (threadIdx.x == 0) part_pw[blockIdx.x] = (double)pw;
       if (!tl_grid_barrier(P.sync, P.status)) return;
@@ -537,9 +704,12 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     A.alpha = (float)alpha;
     A.sigma = (float)(1.0 / sqrt(rr / n));
     A.zscale = zscale_k / A.sigma;
+    A.rest = s_rest;
+    A.rc_part = P.rc_part;
+    A.cshift = P.cshift;
     ZSums sums = {0.0f, 0.0f};
     if (threadIdx.x < 32 * kIssuers) z_issuer_warp(A, T, P.status, threadIdx.x >> 5);
-    else z_worker_warps(A, T, sums, P.status);
+    else z_worker_warps<kCoarse>(A, T, sums, P.status);
     const float t_rr = block_sum(sums.rr, s_red);
     const float t_rz = block_sum(sums.rz, s_red);
     if (threadIdx.x == 0) {
@@ -548,13 +718,24 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     }
     if (!tl_grid_barrier(P.sync, P.status)) return;
     rr = sum_partials(part_rr, G, s_one);
-    const double rz = sum_partials(part_rz, G, s_one);
+    double rz = sum_partials(part_rz, G, s_one);
+    const bool converged = rr <= P.tol2 * rr0 || !(rr == rr) || k >= P.max_iters;
+    if constexpr (kCoarse) {
+      /* z = z_learned + P e_c: r.z gains r_c . e_c; phase P adds P e_c */
+      if (!converged) {
+        phase_c_gemv(P, s_rc);
+        if (!tl_grid_barrier(P.sync, P.status)) return;
+        for (int I = threadIdx.x; I < P.nc; I += blockDim.x) s_ec[I] = __ldcg(P.ec + I);
+        __syncthreads();
+        rz += coarse_dot(s_rc, s_ec, P.nc, s_one);
+      }
+    }
     beta = (k == 0) ? 0.0 : rz / rz_old;
     rz_old = rz;
     par_r ^= 1;
     if (k > 0) par_p ^= 1;
     iters = k;
-    if (rr <= P.tol2 * rr0 || !(rr == rr) || k >= P.max_iters) done = true;
+    if (converged) done = true;
   }
   /* The last step's e += alpha p (every earlier one was added in phase P). */
   if (iters > 0) {
@@ -575,6 +756,7 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
   }
 }
 
+template <bool kCoarse>
 __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ float s_red[kThreads / 32];
@@ -608,7 +790,7 @@ __global__ void __launch_bounds__(kThreads, 1) lpcg_kernel(LpcgParams P) {
   tc05::fence_after_sync();
   T.tmem = *s_tmem;
 
-  lpcg_body(P, T, s_red, &s_one);
+  lpcg_body<kCoarse>(P, T, s_red, &s_one);
 
   /* Teardown: every MMA this block issued has completed (a commit tracks all
    * of the issuing thread's earlier MMAs), then the tensor memory is freed. */
@@ -828,15 +1010,22 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
                                int W, const float* kx, const float* ky, const float* s,
                                float* r, float* r_alt, float* e, float* w, float* z, float* pa,
                                float* pb, double tol, int max_iters, int* iters,
-                               double* rr_final) {
+                               double* rr_final, const tl_coarse_level* coarse) {
   int rc = check_packed_shape(H, W);
   if (rc != TL_OK) return rc;
   TL_REQUIRE(max_iters >= 0 && tol > 0.0, "tl_internal_fpcg_collapsed: bad arguments");
+  if (coarse) {
+    const int b = 1 << coarse->blk_shift;
+    TL_REQUIRE(coarse->nc >= 1 && coarse->nc <= kMaxCoarse && b >= 32 && b <= 128 &&
+                   H % b == 0 && W % b == 0 && coarse->ncx == W / b,
+               "tl_internal_fpcg_collapsed: coarse level does not fit the field");
+  }
   const size_t n = (size_t)H * W;
-  const void* kernel = (const void*)lpcg_kernel;
-  TL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kLpcgSmem));
+  const void* kernel = coarse ? (const void*)lpcg_kernel<true> : (const void*)lpcg_kernel<false>;
+  const int smem = coarse ? kLpcgSmemCoarse : kLpcgSmem;
+  TL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int per_sm = 0;
-  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, kLpcgSmem));
+  TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem));
   TL_REQUIRE(per_sm >= 1, "the learned PCG kernel cannot be resident");
   /* one block per SM: each block holds all 512 tensor-memory columns */
   const int G = ctx->num_sms;
@@ -867,6 +1056,12 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
   P.umma = reinterpret_cast<const __half*>(umma);
   P.kscale = kscale;
   P.part = ctx->d_part;
+  P.cshift = coarse ? coarse->blk_shift : 0;
+  P.ncx = coarse ? coarse->ncx : 0;
+  P.nc = coarse ? coarse->nc : 0;
+  P.ainv = coarse ? coarse->ainv : nullptr;
+  P.rc_part = coarse ? coarse->rc_part : nullptr;
+  P.ec = coarse ? coarse->ec : nullptr;
   P.sync = ctx->d_sync;
   P.status = ctx->d_status;
   P.iters_out = ctx->d_steps;
@@ -876,7 +1071,7 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
   TL_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   ctx->h_steps[0] = -1;
   void* args[] = {&P};
-  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(kThreads), args, kLpcgSmem,
+  TL_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(kThreads), args, smem,
                                       ctx->stream));
   TL_CHECK_LAUNCH(ctx);
   int status = 0;

@@ -250,6 +250,12 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
                                      preconditioner (params->learned) collapsed to
                                      its 17x17 stencil: one persistent kernel,
                                      tensor-core stencil; interior width % 4 == 0 */
+#define TL_METHOD_MIXED_LEARNED_COARSE 5 /* as TL_METHOD_MIXED_LEARNED, with a coarse
+                                     level added to the preconditioner: M^-1 = the
+                                     learned stencil + P (P^T A P)^-1 P^T over
+                                     aggregates of 32, 64 or 128 cells square
+                                     (interior H and W divisible by it, at most 4096
+                                     coarse unknowns; see tl_coarse_inverse) */
 #define TL_METHOD_MIXED_LEARNED_LAYERS 4 /* the same solve applying the network layer
                                      by layer (BF16 convolutions, ~25 launches per
                                      step; H % 4 == 0, W % 64 == 0): the reference
@@ -344,6 +350,18 @@ int tl_net_pcg(tl_net* net, int H, int W, const float* kx, const float* ky, cons
  * (data: device [P][HS][WS]; meta: host int triples). */
 int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, int WS,
                         const int* meta, int B, int H, int W, float* out);
+/* The coarse level of TL_METHOD_MIXED_LEARNED_COARSE for the couplings of a
+ * packed FP32 [H][W] field (kx, ky as for tl_net_pcg): P piecewise constant
+ * on blk x blk aggregates, blk the smallest of 32, 64, 128 that divides H
+ * and W and leaves nc = (H/blk)(W/blk) <= 4096 coarse unknowns (else
+ * TL_ERR_ARG), and Ac = P^T A P assembled from the couplings in FP64. Its
+ * inverse is built on the device (banded Cholesky, then one band solve per
+ * column) and kept in the context, as FP32 rows of nc floats, until H, W or
+ * the couplings change. *blk and *nc receive the aggregate size and the
+ * coarse size; ainv_host (may be NULL; capacity in floats) a copy of the
+ * inverse, row I = Jc * (W/blk) + Ic. No counterpart in the reference. */
+int tl_coarse_inverse(tl_context* ctx, int H, int W, const float* kx, const float* ky,
+                      int* blk, int* nc, float* ainv_host, size_t capacity);
 /* Interior of a field (x*y with halos) to a packed FP32 [H][W] array times
  * scale; and the packed FP32 coefficients with s = D^-1/2. */
 int tl_pack_interior(tl_context* ctx, int x, int y, int halo_depth,

@@ -35,7 +35,7 @@ def _run(name, method, oracle_built, deck=None, **kw):
     c = oracle_built.OracleChunk(d)
     net = None
     try:
-        if method == "mixed-learned":
+        if method.startswith("mixed-learned"):
             from exploringsycl_gb300.learned import Net, load_weights
             net = Net(g.ctx, load_weights()[0])
             kw["learned"] = net
@@ -79,10 +79,11 @@ def _assert_agree(g, c):
         assert abs(sg - sc) <= 1e-7 * abs(sc), (g.summary(), c.summary())
 
 
-# The learned preconditioner needs an interior width divisible by 4; the
-# 75 x 90 deck is refused (TL_ERR_ARG) rather than solved.
-MIXED_CASES = [(n, m) for m in ("mixed", "mixed-jacobi", "mixed-learned") for n in DECKS
-               if not (m == "mixed-learned" and n == "random_odd_75x90")]
+# The learned preconditioner needs an interior width divisible by 4 (and the
+# two-level one sides divisible by 32); the 75 x 90 deck is refused
+# (TL_ERR_ARG) rather than solved. The other decks' sides are multiples of 32.
+MIXED_CASES = [(n, m) for m in ("mixed", "mixed-jacobi", "mixed-learned", "mixed-learned-coarse")
+               for n in DECKS if not (m.startswith("mixed-learned") and n == "random_odd_75x90")]
 
 
 @pytest.mark.parametrize("name,method", MIXED_CASES)
