@@ -594,8 +594,10 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
 /* Two-level kernel, after phase Z's grid barrier: r_c = P^T r_new from the
  * tiles' restriction partials into s_rc (every block assembles the whole
  * vector, in the same order), then this block's share of the rows of
- * e_c = Ac^-1 r_c into P.ec, one warp per row, FP32 sums in a fixed order. */
-__device__ __forceinline__ void phase_c_gemv(const LpcgParams& P, float* s_rc) {
+ * e_c = Ac^-1 r_c into P.ec, one warp per row, FP32 sums in a fixed order.
+ * Returns (in every thread) the block's part of r_c . e_c over its rows,
+ * summed in a fixed order. */
+__device__ __forceinline__ float phase_c_gemv(const LpcgParams& P, float* s_rc, float* s_red) {
   const int b = 1 << P.cshift;
   const int arows = b < kTH ? b : kTH, acols = b < kTW ? b : kTW;
   const int ncol = kTW / acols;
@@ -612,12 +614,14 @@ __device__ __forceinline__ void phase_c_gemv(const LpcgParams& P, float* s_rc) {
   const int rows = (P.nc + (int)gridDim.x - 1) / (int)gridDim.x;
   const int r0 = blockIdx.x * rows, r1 = min(P.nc, r0 + rows);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float dot = 0.0f;
   for (int I = r0 + warp; I < r1; I += (int)(blockDim.x >> 5)) {
     const float* row = P.ainv + (size_t)I * P.nc;
     float acc = 0.0f;
     if ((P.nc & 3) == 0) {
       const float4* row4 = reinterpret_cast<const float4*>(row);
       const float4* rc4 = reinterpret_cast<const float4*>(s_rc);
+#pragma unroll 8
       for (int q = lane; q < (P.nc >> 2); q += 32) {
         const float4 a = __ldg(row4 + q);
         const float4 r = rc4[q];
@@ -628,23 +632,9 @@ __device__ __forceinline__ void phase_c_gemv(const LpcgParams& P, float* s_rc) {
     }
     acc = warp_sum(acc);
     if (lane == 0) P.ec[I] = acc;
+    dot += acc * s_rc[I];
   }
-}
-
-/* r_c . e_c in double, in one fixed order, the same in every block. */
-__device__ __forceinline__ double coarse_dot(const float* s_rc, const float* s_ec, int nc,
-                                             double* s_one) {
-  if (threadIdx.x < 32) {
-    double v = 0.0;
-    for (int i = threadIdx.x; i < nc; i += 32) v += (double)s_rc[i] * (double)s_ec[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TL_FULL_MASK, v, o);
-    if (threadIdx.x == 0) *s_one = v;
-  }
-  __syncthreads();
-  const double t = *s_one;
-  __syncthreads();
-  return t;
+  return block_sum(lane == 0 ? dot : 0.0f, s_red);
 }
 
 /* The solve; returns when done or when a wait ran out (status set). */
@@ -663,6 +653,7 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
   double* part_pw = P.part;
   double* part_rr = P.part + G;
   double* part_rz = P.part + 2 * G;
+  double* part_ce = P.part + 3 * G;  /* two-level kernel: the blocks' r_c . e_c */
 
   /* r.r of the incoming residual: its RMS sets the FP16 staging scale. */
   {
@@ -723,11 +714,11 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
     if constexpr (kCoarse) {
       /* z = z_learned + P e_c: r.z gains r_c . e_c; phase P adds P e_c */
       if (!converged) {
-        phase_c_gemv(P, s_rc);
+        const float dot = phase_c_gemv(P, s_rc, s_red);
+        if (threadIdx.x == 0) part_ce[blockIdx.x] = (double)dot;
         if (!tl_grid_barrier(P.sync, P.status)) return;
         for (int I = threadIdx.x; I < P.nc; I += blockDim.x) s_ec[I] = __ldcg(P.ec + I);
-        __syncthreads();
-        rz += coarse_dot(s_rc, s_ec, P.nc, s_one);
+        rz += sum_partials(part_ce, G, s_one);  /* its barrier also publishes s_ec */
       }
     }
     beta = (k == 0) ? 0.0 : rz / rz_old;
