@@ -7,10 +7,12 @@ uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
 1/density; each timestep solved until the FP64 true residual satisfies
 ||u0 - A u||_2 <= 1e-10 ||u0||_2, with the learned + mixed-precision solver:
 FP32 inner PCG whose preconditioner is the trained network collapsed
-to one 17x17 stencil (tensor cores), inside FP64 iterative refinement. The
-same timesteps are also solved, under the same stop rule, with plain FP64 CG
-in both arithmetic contracts (exact / fused multiply-add) and with the
-mixed-precision Jacobi-PCG solver (the `compare` list). A step is one
+to one 17x17 stencil (tensor cores) plus a coarse level (64 x 64-cell
+aggregates, the dense FP32 inverse of P^T A P applied every step), inside
+FP64 iterative refinement. The same timesteps are also solved, under the
+same stop rule, with plain FP64 CG in both arithmetic contracts (exact /
+fused multiply-add), with the mixed-precision Jacobi-PCG solver and with the
+learned PCG without the coarse level (the `compare` list). A step is one
 timestep (TeaLeaf/diffuse.c:23-78): halo update, the solve, residual / norm /
 finalise, and the field summary. Timesteps follow one another: the W warm-up
 steps are timesteps 1..W and the K timed steps are timesteps W+1..W+K, in
@@ -28,8 +30,10 @@ Reported:
   iters_per_s  solver steps (CG or inner PCG steps) per second of `value`
   roofline   the dominant kernel (the persistent inner FP32 kernel of the
              mixed solver, or the FP64 CG kernel for plain/cg64): algorithmic
-             bytes / kernel time against the measured HBM copy bandwidth; for
-             the FP64 kernel also FP64 instructions / s against the FP64 peak
+             bytes / kernel time against the measured HBM copy bandwidth (the
+             learned kernel's 52 B per cell and step, plus the coarse inverse's
+             4 nc^2 bytes per step with the coarse level); for the FP64 kernel
+             also FP64 instructions / s against the FP64 peak
   solve.error_vs_fp64  the headline solver's u and field summary against
              plain FP64 CG (exact contract, bit-identical to the CPU oracle)
              on the same timesteps
@@ -562,7 +566,7 @@ def main() -> None:
     ap.add_argument("--deck", choices=["random", "two-state"], default="random")
     ap.add_argument("--solver", choices=["mixed-jacobi", "mixed", "mixed-learned",
                                          "mixed-learned-coarse", "cg64", "plain"],
-                    default="mixed-learned")
+                    default="mixed-learned-coarse")
     ap.add_argument("--fp64", choices=["exact", "fused"], default="exact",
                     help="arithmetic contract of the persistent FP64 CG (plain, cg64, fall-back)")
     ap.add_argument("--inner-tol", type=float, default=0.0,
