@@ -104,10 +104,11 @@ FP64_PIPE_OPS_PER_CELL_STEP = {"exact": 9, "fused": 9}
 # dram__bytes_read.sum + dram__bytes_write.sum per interior cell per step of
 # each persistent kernel, from one ncu capture (profiles/*.txt).
 NCU_BYTES_PER_CELL_STEP = {
-    ("cg_persistent_kernel", "exact"): 116.9,  # profiles/cg_persistent_fp64_exact_4096.txt
-    ("cg_persistent_kernel", "fused"): 120.1,  # profiles/cg_persistent_fp64_fused_4096.txt
-    ("inner_cg_kernel", None): 51.3,           # profiles/inner_cg_mixed_jacobi_4096.txt
-    ("lpcg_kernel", None): 51.3,               # profiles/lpcg_learned_4096.txt
+    ("cg_persistent_kernel", "exact"): 117.3,      # profiles/cg_persistent_fp64_exact_4096.txt
+    ("cg_persistent_kernel", "fused"): 115.0,      # profiles/cg_persistent_fp64_fused_4096.txt
+    ("inner_cg_kernel", None): 51.3,               # profiles/inner_cg_mixed_jacobi_4096.txt
+    ("lpcg_kernel", "mixed-learned"): 51.1,        # profiles/lpcg_learned_4096.txt
+    ("lpcg_kernel", "mixed-learned-coarse"): 55.7,  # profiles/lpcg_coarse_4096.txt
 }
 RANDOM_SEED = 1
 REL_TOL = 1e-10
@@ -475,8 +476,9 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         kernel, bpc = "inner_cg_kernel", INNER_BYTES[args.solver]
     achieved = bpc * cells * k_steps / (k_ms * 1e-3) / 1e9
     traffic = None
-    key = (kernel, args.fp64 if kernel == "cg_persistent_kernel" else None)
-    if args.solver != "mixed-learned-coarse" and NCU_BYTES_PER_CELL_STEP.get(key) is not None:
+    key = (kernel, args.fp64 if kernel == "cg_persistent_kernel" else
+           args.solver if kernel == "lpcg_kernel" else None)
+    if args.size == 4096 and NCU_BYTES_PER_CELL_STEP.get(key) is not None:
         # ncu DRAM bytes per cell and step x the cells and steps of one timestep
         traffic = NCU_BYTES_PER_CELL_STEP[key] * cells * k_steps
     roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"],
