@@ -8,7 +8,8 @@ uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
 ||u0 - A u||_2 <= 1e-10 ||u0||_2, with the learned + mixed-precision solver:
 FP32 inner PCG whose preconditioner is the trained network collapsed
 to one 17x17 stencil (tensor cores) plus a coarse level (64 x 64-cell
-aggregates, the dense FP32 inverse of P^T A P applied every step), inside
+aggregates, the dense inverse of P^T A P, stored as FP16 scaled by a power
+of two, applied every step), inside
 FP64 iterative refinement. The same timesteps are also solved, under the
 same stop rule, with plain FP64 CG in both arithmetic contracts (exact /
 fused multiply-add), with the mixed-precision Jacobi-PCG solver and with the
@@ -90,9 +91,9 @@ def coarse_unknowns(size: int) -> int:
 
 def learned_bytes(solver: str, size: int) -> float:
     """Algorithmic bytes per cell and inner step; the two-level step also
-    reads the FP32 inverse of the coarse operator once (4 nc^2 bytes)."""
+    reads the FP16 inverse of the coarse operator once (2 nc^2 bytes)."""
     if solver == "mixed-learned-coarse":
-        return LEARNED_BYTES + 4.0 * coarse_unknowns(size) ** 2 / (size * size)
+        return LEARNED_BYTES + 2.0 * coarse_unknowns(size) ** 2 / (size * size)
     return LEARNED_BYTES
 # FP64 operations per cell of one CG step: exact contract (stencil 9 with the
 # precomputed diagonal, dot products 2 x 1.6, u/r update 4, p update 2) and fused
@@ -202,7 +203,7 @@ def config_for(args, steps_per_timestep=None) -> dict:
                                "(network collapsed to a 17x17 stencil on the tensor cores) "
                                "in FP64 iterative refinement",
               "mixed-learned-coarse": "FP32 inner PCG with the learned preconditioner plus "
-                                      "a coarse level (aggregates, dense FP32 inverse of "
+                                      "a coarse level (aggregates, dense FP16 inverse of "
                                       "P^T A P) in FP64 iterative refinement",
               }[args.solver]
     return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "

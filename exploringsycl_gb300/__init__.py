@@ -139,6 +139,7 @@ HANDLE_FIRST = {
     "tl_pack_interior": [_I, _I, _I, _P, _D, _P],
     "tl_pack_coefficients": [_I, _I, _I, _P, _P, _P, _P, _P],
     "tl_coarse_inverse": [_I, _I, _P, _P, _PI, _PI, C.POINTER(C.c_float), C.c_size_t],
+    "tl_coarse_inverse_f16": [_I, _I, _P, _P, C.POINTER(C.c_uint16), C.c_size_t, _PI],
 }
 
 _lib = None

@@ -10,8 +10,12 @@
  * at 4096 unknowns or fewer and divides H and W, so that they line up with
  * the 128 x 64 tiles of the learned PCG kernel: a tile's epilogue sums its
  * aggregates' residuals (the restriction) without another pass over memory,
- * and one dense product with the FP32 inverse Ac^-1 (64 MB at 4096
- * unknowns) gives the coarse correction every step.
+ * and one dense product with the inverse Ac^-1 gives the coarse correction
+ * every step. The product reads an FP16 copy of the inverse (32 MB at 4096
+ * unknowns), scaled by a power of two so that its largest entry lies in
+ * [2^14, 2^15): the rounding moves an entry by at most 2^-11 of itself or
+ * 2^-39 of the largest entry, whichever is larger (the second bound holds
+ * for the tiny entries far from the diagonal, FP16 subnormals once scaled).
  *
  * Ac = P^T A P needs no product with A. For A = I + L (L the weighted graph
  * Laplacian of the couplings, zero flux at the field's edges) the diagonal of
@@ -29,6 +33,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <string>
 #include <vector>
@@ -120,6 +125,25 @@ __global__ void coarse_inverse_kernel(int n, int bw, const double* __restrict__ 
     work[(size_t)i * n + j] = x;
     ainv[(size_t)i * n + j] = (float)x;
   }
+}
+
+/* Largest |entry| of the inverse: non-negative floats order like their bit
+ * patterns (a NaN orders above every finite value and is caught by the host). */
+__global__ void coarse_absmax_kernel(const float* __restrict__ a, size_t n, unsigned* out) {
+  unsigned m = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    m = max(m, __float_as_uint(fabsf(a[i])));
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+/* The FP16 copy: a * 2^e (exact in FP32) rounded to nearest. */
+__global__ void coarse_half_kernel(const float* __restrict__ a, size_t n, float scale,
+                                   __half* out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = __float2half_rn(a[i] * scale);
 }
 
 /* Banded Cholesky of the 5-point coarse matrix (bandwidth bw = ncx) into
@@ -232,7 +256,32 @@ int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, c
     coarse_inverse_kernel<<<(nc + 31) / 32, 32, 0, ctx->stream>>>(nc, bw, band_d, work,
                                                                   ctx->d_ainv);
     TL_CHECK_LAUNCH(ctx);
+    /* the FP16 copy, scaled by 2^e: the largest entry m 2^k (m in [0.5, 1))
+     * becomes m 2^15 */
+    unsigned* d_max = reinterpret_cast<unsigned*>(ctx->d_hash);
+    TL_CUDA(cudaMemsetAsync(d_max, 0, sizeof(unsigned), ctx->stream));
+    coarse_absmax_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->d_ainv, nn, d_max);
+    TL_CHECK_LAUNCH(ctx);
+    unsigned max_bits = 0;
+    TL_CUDA(cudaMemcpyAsync(&max_bits, d_max, sizeof(max_bits), cudaMemcpyDeviceToHost,
+                            ctx->stream));
     TL_CUDA(cudaStreamSynchronize(ctx->stream));
+    float amax;
+    memcpy(&amax, &max_bits, sizeof(amax));
+    int k = 0;
+    if (isfinite(amax) && amax > 0.0f) frexpf(amax, &k);
+    const int e = 15 - k;
+    if (!(isfinite(amax) && amax > 0.0f) || e > 126 || e < -126) {
+      return tl_set_error(TL_ERR_NUMERIC, "coarse inverse out of the FP16 copy's range");
+    }
+    rc = ensure(&ctx->d_ainv16, &ctx->ainv16_cap, nn, ctx->stream);
+    if (rc != TL_OK) return rc;
+    coarse_half_kernel<<<4 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->d_ainv, nn,
+                                                                 ldexpf(1.0f, e),
+                                                                 ctx->d_ainv16);
+    TL_CHECK_LAUNCH(ctx);
+    TL_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->coarse_exp = e;
     ctx->coarse_H = H;
     ctx->coarse_W = W;
     ctx->coarse_blk = 1 << sh;
@@ -243,6 +292,8 @@ int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, c
   out->ncy = ncy;
   out->nc = nc;
   out->ainv = ctx->d_ainv;
+  out->ainv16 = ctx->d_ainv16;
+  out->exp16 = ctx->coarse_exp;
   out->rc_part = ctx->d_coarse_vec;
   out->ec = ctx->d_coarse_vec + tiles * kRestrictSlots;
   return TL_OK;
@@ -262,6 +313,26 @@ extern "C" int tl_coarse_inverse(tl_context* ctx, int H, int W, const float* kx,
     TL_REQUIRE(capacity >= nn, "tl_coarse_inverse: host array too small");
     TL_CUDA(cudaMemcpyAsync(ainv_host, lv.ainv, nn * sizeof(float), cudaMemcpyDeviceToHost,
                             ctx->stream));
+    TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return TL_OK;
+}
+
+extern "C" int tl_coarse_inverse_f16(tl_context* ctx, int H, int W, const float* kx,
+                                     const float* ky, uint16_t* half_host, size_t capacity,
+                                     int* exp2) {
+  TL_REQUIRE(ctx && kx && ky && exp2, "tl_coarse_inverse_f16: null argument");
+  TL_REQUIRE(H >= 1 && W >= 1 && (size_t)H * W < (1ull << 31),
+             "tl_coarse_inverse_f16: bad shape");
+  tl_coarse_level lv;
+  int rc = tl_internal_coarse_prepare(ctx, H, W, kx, ky, &lv);
+  if (rc != TL_OK) return rc;
+  *exp2 = lv.exp16;
+  if (half_host) {
+    const size_t nn = (size_t)lv.nc * lv.nc;
+    TL_REQUIRE(capacity >= nn, "tl_coarse_inverse_f16: host array too small");
+    TL_CUDA(cudaMemcpyAsync(half_host, lv.ainv16, nn * sizeof(uint16_t),
+                            cudaMemcpyDeviceToHost, ctx->stream));
     TL_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   return TL_OK;

@@ -90,6 +90,7 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_diag);
   cudaFree(ctx->d_f32);
   cudaFree(ctx->d_ainv);
+  cudaFree(ctx->d_ainv16);
   cudaFree(ctx->d_coarse_work);
   cudaFree(ctx->d_coarse_vec);
   cudaFree(ctx->d_hash);

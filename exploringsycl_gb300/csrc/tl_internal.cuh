@@ -22,6 +22,7 @@
  */
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -84,10 +85,14 @@ struct tl_context {
   tl_solve_stats last_solve = {0.0f, 0, 0};
   int fp64_fused = 0;             /* TL_FP64_FUSED: the persistent FP64 CG uses FMAs */
   /* coarse level of the two-level learned PCG (tl_coarse.cu): the FP32
-   * inverse of the coarse operator of the couplings last seen, kept while
-   * they do not change, and its per-step vectors */
+   * inverse of the coarse operator of the couplings last seen and the FP16
+   * copy the kernel reads, kept while they do not change, and its per-step
+   * vectors */
   float* d_ainv = nullptr;        /* nc x nc, row-major */
   size_t ainv_cap = 0;
+  __half* d_ainv16 = nullptr;     /* the same times 2^coarse_exp, FP16 */
+  size_t ainv16_cap = 0;
+  int coarse_exp = 0;
   double* d_coarse_work = nullptr; /* the inverse's FP64 columns, then the bands */
   size_t coarse_work_cap = 0;
   float* d_coarse_vec = nullptr;  /* tile restriction partials, then e_c */
@@ -99,11 +104,15 @@ struct tl_context {
 
 /* The coarse level of a packed [H][W] field: blk x blk aggregates
  * (blk = 1 << blk_shift), an ncx x ncy coarse grid of nc unknowns, the
- * inverse of its operator P^T A P (FP32, row-major nc x nc), the per-tile
- * restriction partials (8 per 128 x 64 tile) and the coarse correction e_c. */
+ * inverse of its operator P^T A P (FP32, row-major nc x nc) and its FP16
+ * copy (entries times 2^exp16, so that the largest lies in [2^14, 2^15)),
+ * the per-tile restriction partials (8 per 128 x 64 tile) and the coarse
+ * correction e_c. */
 struct tl_coarse_level {
   int blk_shift, ncx, ncy, nc;
   const float* ainv;
+  const __half* ainv16;
+  int exp16;
   float* rc_part;
   float* ec;
 };

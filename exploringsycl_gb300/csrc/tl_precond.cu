@@ -128,10 +128,12 @@ struct LpcgParams {
   const float* kscale;
   double* part;  /* 3 arrays of gridDim.x partial sums: p.w, r.r, r.z */
   /* coarse level (two-level kernel only): blk = 1 << cshift aggregates on an
-   * ncx-wide coarse grid of nc unknowns, Ac^-1 (FP32, nc x nc), the tiles'
-   * restriction partials (8 per tile) and the correction e_c */
+   * ncx-wide coarse grid of nc unknowns, Ac^-1 as FP16 (nc x nc, entries
+   * times 2^e; ainv_unscale = 2^-e), the tiles' restriction partials (8 per
+   * tile) and the correction e_c */
   int cshift, ncx, nc;
-  const float* ainv;
+  const __half* ainv;
+  float ainv_unscale;
   float* rc_part;
   float* ec;
   unsigned* sync;
@@ -594,7 +596,8 @@ __device__ __forceinline__ void z_worker_warps(const ZArgs& A, TileState& T, ZSu
 /* Two-level kernel, after phase Z's grid barrier: r_c = P^T r_new from the
  * tiles' restriction partials into s_rc (every block assembles the whole
  * vector, in the same order), then this block's share of the rows of
- * e_c = Ac^-1 r_c into P.ec, one warp per row, FP32 sums in a fixed order.
+ * e_c = Ac^-1 r_c into P.ec, one warp per row: the FP16 entries widened to
+ * FP32, FP32 sums in a fixed order, times 2^-e at the end (exact).
  * Returns (in every thread) the block's part of r_c . e_c over its rows,
  * summed in a fixed order. */
 __device__ __forceinline__ float phase_c_gemv(const LpcgParams& P, float* s_rc, float* s_red) {
@@ -616,21 +619,25 @@ __device__ __forceinline__ float phase_c_gemv(const LpcgParams& P, float* s_rc, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float dot = 0.0f;
   for (int I = r0 + warp; I < r1; I += (int)(blockDim.x >> 5)) {
-    const float* row = P.ainv + (size_t)I * P.nc;
+    const __half* row = P.ainv + (size_t)I * P.nc;
     float acc = 0.0f;
-    if ((P.nc & 3) == 0) {
-      const float4* row4 = reinterpret_cast<const float4*>(row);
+    if ((P.nc & 7) == 0) {  /* 16-byte rows: eight entries per load */
+      const uint4* row8 = reinterpret_cast<const uint4*>(row);
       const float4* rc4 = reinterpret_cast<const float4*>(s_rc);
-#pragma unroll 8
-      for (int q = lane; q < (P.nc >> 2); q += 32) {
-        const float4 a = __ldg(row4 + q);
-        const float4 r = rc4[q];
-        acc += a.x * r.x + a.y * r.y + a.z * r.z + a.w * r.w;
+#pragma unroll 4
+      for (int q = lane; q < (P.nc >> 3); q += 32) {
+        const uint4 a = __ldg(row8 + q);
+        const __half2* h = reinterpret_cast<const __half2*>(&a);
+        const float2 a0 = __half22float2(h[0]), a1 = __half22float2(h[1]);
+        const float2 a2 = __half22float2(h[2]), a3 = __half22float2(h[3]);
+        const float4 ra = rc4[2 * q], rb = rc4[2 * q + 1];
+        acc += a0.x * ra.x + a0.y * ra.y + a1.x * ra.z + a1.y * ra.w + a2.x * rb.x +
+               a2.y * rb.y + a3.x * rb.z + a3.y * rb.w;
       }
     } else {
-      for (int q = lane; q < P.nc; q += 32) acc += __ldg(row + q) * s_rc[q];
+      for (int q = lane; q < P.nc; q += 32) acc += __half2float(row[q]) * s_rc[q];
     }
-    acc = warp_sum(acc);
+    acc = warp_sum(acc) * P.ainv_unscale;
     if (lane == 0) P.ec[I] = acc;
     dot += acc * s_rc[I];
   }
@@ -1050,7 +1057,8 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
   P.cshift = coarse ? coarse->blk_shift : 0;
   P.ncx = coarse ? coarse->ncx : 0;
   P.nc = coarse ? coarse->nc : 0;
-  P.ainv = coarse ? coarse->ainv : nullptr;
+  P.ainv = coarse ? coarse->ainv16 : nullptr;
+  P.ainv_unscale = coarse ? ldexpf(1.0f, -coarse->exp16) : 0.0f;
   P.rc_part = coarse ? coarse->rc_part : nullptr;
   P.ec = coarse ? coarse->ec : nullptr;
   P.sync = ctx->d_sync;

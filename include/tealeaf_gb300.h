@@ -37,6 +37,7 @@
 #define TEALEAF_GB300_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -362,6 +363,13 @@ int tl_net_gather_crops(tl_context* ctx, const float* data, int HS, int WS,
  * inverse, row I = Jc * (W/blk) + Ic. No counterpart in the reference. */
 int tl_coarse_inverse(tl_context* ctx, int H, int W, const float* kx, const float* ky,
                       int* blk, int* nc, float* ainv_host, size_t capacity);
+/* The copy of the same inverse that the two-level kernel reads: every entry
+ * times 2^(*exp2) rounded to FP16 (round to nearest even), *exp2 chosen so
+ * that the largest entry lies in [2^14, 2^15). half_host (may be NULL;
+ * capacity in entries) receives the nc x nc FP16 bit patterns. No
+ * counterpart in the reference. */
+int tl_coarse_inverse_f16(tl_context* ctx, int H, int W, const float* kx, const float* ky,
+                          uint16_t* half_host, size_t capacity, int* exp2);
 /* Interior of a field (x*y with halos) to a packed FP32 [H][W] array times
  * scale; and the packed FP32 coefficients with s = D^-1/2. */
 int tl_pack_interior(tl_context* ctx, int x, int y, int halo_depth,

@@ -5,7 +5,10 @@ two-level solve reaches the FP64 target in fewer inner steps than the
 learned PCG alone, agrees with the oracle's FP64 CG, and is bit-reproducible.
 
 Tolerance of the inverse: it is built in FP64 and stored in FP32, so its
-entries agree with the oracle's to 1e-5 of the largest one."""
+entries agree with the oracle's to 1e-5 of the largest one. The FP16 copy the
+kernel reads is the FP32 inverse times 2^e rounded to nearest: within 2^-11
+of each entry (2^-25 times 2^-e below FP16's normal range), the largest
+entry scaled into [2^14, 2^15)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -47,6 +50,31 @@ def test_coarse_inverse_matches_oracle(H, W, blk, backend_built):
     for a, (x, y) in ((ainv, (kx, ky)), (ainv2, (ky, kx))):
         want = np.linalg.inv(co.coarse_operator(x.astype(np.float64), y.astype(np.float64), blk))
         assert np.max(np.abs(a - want)) <= 1e-5 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("H,W", [(256, 256), (2304, 4096)])
+def test_fp16_copy_is_the_rounded_inverse(H, W, backend_built):
+    from exploringsycl_gb300 import Context
+    rng = np.random.default_rng(7 * H + W)
+    kx = (10.0 ** rng.uniform(-1, 3, (H, W))).astype(np.float32)
+    ky = (10.0 ** rng.uniform(-1, 3, (H, W))).astype(np.float32)
+    with Context(0) as ctx:
+        _, ainv = _coarse_inverse(ctx, kx, ky)
+        dkx, dky = ctx.alloc_f32(kx.size), ctx.alloc_f32(ky.size)
+        ctx.upload_f32(dkx, kx)
+        ctx.upload_f32(dky, ky)
+        half = np.empty(ainv.size, np.uint16)
+        e = C.c_int(0)
+        ctx.call("tl_coarse_inverse_f16", H, W, dkx, dky,
+                 half.ctypes.data_as(C.POINTER(C.c_uint16)), half.size, C.byref(e))
+    got = half.view(np.float16).astype(np.float64).reshape(ainv.shape)
+    a = ainv.astype(np.float64)
+    assert 2.0 ** 14 <= np.max(np.abs(got)) < 2.0 ** 15
+    err = np.abs(np.ldexp(got, -e.value) - a)
+    assert np.all(err <= 2.0 ** -11 * np.abs(a) + 2.0 ** (-25 - e.value))
+    # round to nearest: equal to numpy's conversion of the same scaled values
+    assert np.array_equal(half.reshape(a.shape),
+                          np.ldexp(a, e.value).astype(np.float16).view(np.uint16))
 
 
 def test_coarse_level_refuses_fields_without_aggregates(backend_built):
