@@ -9,11 +9,14 @@ uniform in [1e-4, 25]; splitmix64 seed 1), dt 0.004, conductivity =
 FP32 inner PCG whose preconditioner is the trained network collapsed
 to one 17x17 stencil (tensor cores) plus a coarse level (64 x 64-cell
 aggregates, the dense inverse of P^T A P, stored as FP16 scaled by a power
-of two, applied every step), inside
-FP64 iterative refinement. The same timesteps are also solved, under the
-same stop rule, with plain FP64 CG in both arithmetic contracts (exact /
-fused multiply-add), with the mixed-precision Jacobi-PCG solver and with the
-learned PCG without the coarse level (the `compare` list). A step is one
+of two, applied every step), inside FP64 iterative refinement, started from
+the A-norm best combination of u0 and the last 7 solutions (successive
+right-hand sides; `--projection 0` starts from u0 as the reference does).
+The same timesteps are also solved, under the same stop rule, with plain
+FP64 CG from u0 in both arithmetic contracts (exact / fused multiply-add),
+with the mixed-precision Jacobi-PCG, the learned PCG and the two-level
+learned PCG started from u0, and with plain FP64 CG started from the same
+projection (the `compare` list). A step is one
 timestep (TeaLeaf/diffuse.c:23-78): halo update, the solve, residual / norm /
 finalise, and the field summary. Timesteps follow one another: the W warm-up
 steps are timesteps 1..W and the K timed steps are timesteps W+1..W+K, in
@@ -33,8 +36,10 @@ Reported:
              mixed solver, or the FP64 CG kernel for plain/cg64): algorithmic
              bytes / kernel time against the measured HBM copy bandwidth (the
              learned kernel's 52 B per cell and step, plus the coarse inverse's
-             4 nc^2 bytes per step with the coarse level); for the FP64 kernel
+             2 nc^2 bytes per step with the coarse level); for the FP64 kernel
              also FP64 instructions / s against the FP64 peak
+  solve      per timestep: outer and inner steps, the starting guess's
+             relative residual and basis size, fall-backs
   solve.error_vs_fp64  the headline solver's u and field summary against
              plain FP64 CG (exact contract, bit-identical to the CPU oracle)
              on the same timesteps
@@ -184,6 +189,15 @@ def deck_for(size: int, kind: str = "random"):
                           max_iters=MAX_ITERS)
 
 
+def projection_for(args, solver: str) -> int:
+    """Solutions kept for the starting guess of the given solver."""
+    if solver == "plain":
+        return 0
+    if args.projection >= 0:
+        return args.projection
+    return 0 if solver == "cg64" else 7
+
+
 def stop_rule(solver: str) -> str:
     if solver == "plain":
         return f"sqrt(|rr|) < 1e-15 (the reference's absolute rule), max_iters {MAX_ITERS}"
@@ -211,6 +225,9 @@ def config_for(args, steps_per_timestep=None) -> dict:
             "cells": args.size * args.size, "halo_depth": 2, "dt": 0.004,
             "deck": args.deck, "solver": args.solver, "stop": stop_rule(args.solver),
             "max_iters": MAX_ITERS,
+            "start": (f"A-norm best combination of u0 and the last {projection_for(args, args.solver)}"
+                      " solutions of this run (successive right-hand sides)"
+                      if projection_for(args, args.solver) else "u0 (the reference's x0 = b)"),
             "timed_timesteps": [args.warmup + 1, args.warmup + args.steps],
             "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2)"
                   if args.size >= 4096 else "fields smaller than L2 at this size",
@@ -298,9 +315,11 @@ def max_over_ranks(values: list[float], dist) -> list[float]:
 class Stepper:
     """One chunk and the timestep of the chosen solver."""
 
-    def __init__(self, args, solver: str, ctx, contract: str | None = None):
+    def __init__(self, args, solver: str, ctx, contract: str | None = None,
+                 projection: int | None = None):
         from exploringsycl_gb300.chunk import GpuChunk
         self.contract = contract or args.fp64
+        self.projection = projection_for(args, solver) if projection is None else projection
         ctx.set_fp64_contract(self.contract)
         self.solver = solver
         self.chunk = GpuChunk(deck_for(args.size, args.deck), ctx=ctx)
@@ -324,7 +343,8 @@ class Stepper:
         else:
             rep = self.chunk.solve_timestep(self.solver, rel_tol=REL_TOL,
                                             inner_tol=self.inner_tol, learned=self.net,
-                                            max_inner=self.max_inner, max_outer=self.max_outer)
+                                            max_inner=self.max_inner, max_outer=self.max_outer,
+                                            projection=self.projection)
             out = {"kernel_ms": rep["inner_kernel_ms"],
                    "kernel_steps": rep["inner_steps"] + rep["fallback_steps"],
                    "cg_steps": rep["inner_steps"] + rep["fallback_steps"], "report": rep}
@@ -366,15 +386,26 @@ def timed_steps(stepper, steps: int, stream, barrier, sample_clocks: bool, devic
     return evs[0].elapsed_time(evs[-1]), per, stepper.ctx.launches() - launches0, clocks
 
 
-def e2e_steps(stepper, energy0: np.ndarray, steps: int, barrier) -> tuple[list[float], list]:
+def e2e_steps(stepper, energy_start: np.ndarray, energy_w: np.ndarray, warmup: int,
+              steps: int, barrier) -> tuple[list[float], list]:
     """The timed timesteps again, from the state they started from, through
     the C ABI with host buffers: each step copies density and energy in from
-    pinned host memory, solves, and copies energy back (host wall clock)."""
+    pinned host memory, solves, and copies energy back (host wall clock).
+    With a projected starting guess the solutions that the solver keeps are
+    part of that state: they are dropped and timesteps 1..W replayed
+    (untimed) first, so that the timed solves see the same ones as before."""
     import torch
 
     from exploringsycl_gb300 import check
     chunk, lib, ctx = stepper.chunk, stepper.ctx.lib, stepper.ctx
     n = chunk.n
+    if stepper.projection:
+        ctx.call("tl_projection_reset")
+        h_start = torch.from_numpy(energy_start).pin_memory()
+        check(lib.tl_copy_to_device(ctx.h, chunk.f["energy"], h_start.data_ptr(), n), "copy")
+        for _ in range(warmup):
+            stepper.step()
+    energy0 = energy_w
     h_density = torch.empty(n, dtype=torch.float64, pin_memory=True)
     h_energy = torch.from_numpy(energy0).pin_memory()
     check(lib.tl_copy_to_host(ctx.h, h_density.data_ptr(), chunk.f["density"], n), "copy")
@@ -419,12 +450,14 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         if dist is not None:
             dist.barrier()
 
+    energy_0 = main.energy()          # the deck's initial state
     warm = [main.step() for _ in range(args.warmup)]
     torch.cuda.synchronize()
     energy_w = main.energy()          # state at the start of the timed window
     total_ms, per, launches, clocks = timed_steps(main, args.steps, stream, barrier, True, local)
     u_main = interior(chunk, chunk.read("u"))
-    e2e_times, e2e_summaries = e2e_steps(main, energy_w, args.steps, barrier)
+    e2e_times, e2e_summaries = e2e_steps(main, energy_0, energy_w, args.warmup, args.steps,
+                                         barrier)
     e2e_same = e2e_summaries == [p["summary"] for p in per]
 
     # The same timesteps with the other solvers under the same stop rule:
@@ -435,19 +468,24 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     if args.solver in ("plain", "cg64") and args.fp64 == "exact":
         fp64_ref = (energy_w, per, u_main)
     if args.compare and args.solver not in ("plain", "cg64"):
-        others = [("cg64", "exact", "plain FP64 CG (exact contract, bit-identical to the "
-                                    "oracle), same stop rule"),
-                  ("cg64", "fused", "plain FP64 CG (fused multiply-add contract), "
-                                    "same stop rule")]
+        others = [("cg64", "exact", 0, "plain FP64 CG (exact contract, bit-identical to the "
+                                       "oracle), same stop rule"),
+                  ("cg64", "fused", 0, "plain FP64 CG (fused multiply-add contract), "
+                                       "same stop rule")]
         for solver in ("mixed-jacobi", "mixed-learned", "mixed-learned-coarse"):
-            if solver != args.solver:
-                others.append((solver, args.fp64, f"{solver}, same stop rule"))
-        for solver, contract, label in others:
+            if solver != args.solver or main.projection:
+                others.append((solver, args.fp64, 0, f"{solver}, started from u0, "
+                                                     "same stop rule"))
+        if main.projection:
+            others.append(("cg64", "exact", main.projection,
+                           f"plain FP64 CG (exact contract) started from the same projection "
+                           f"(last {main.projection} solutions), same stop rule"))
+        for solver, contract, proj, label in others:
             ctx2 = Context(device=local)
-            other = Stepper(args, solver, ctx2, contract)
+            other = Stepper(args, solver, ctx2, contract, proj)
             cwarm = [other.step() for _ in range(args.warmup)]
             torch.cuda.synchronize()
-            e_w = other.energy() if (solver, contract) == ("cg64", "exact") else None
+            e_w = other.energy() if (solver, contract, proj) == ("cg64", "exact", 0) else None
             stream2 = torch.cuda.ExternalStream(ctx2.stream(), device=local)
             c_ms, c_per, _, _ = timed_steps(other, args.steps, stream2, barrier, False, local)
             csteps = [p["cg_steps"] for p in c_per]
@@ -518,7 +556,9 @@ def run_ours(args, rank: int, world: int, dist) -> None:
             "outer_steps": [r["outer_steps"] for r in reports],
             "inner_steps": [r["inner_steps"] for r in reports],
             "fallback_events": sum(r["fallback_events"] for r in reports),
-            "final_rel_residual_max": max(r["final_rel_residual"] for r in reports)}
+            "final_rel_residual_max": max(r["final_rel_residual"] for r in reports),
+            "initial_rel_residual": [r["initial_rel_residual"] for r in reports],
+            "projection_basis": [r["projection_basis"] for r in reports]}
     if fp64_ref is not None and args.solver not in ("plain", "cg64"):
         _, ref_per, u_ref = fp64_ref
         names = ("volume", "mass", "internal_energy", "temperature")
@@ -577,6 +617,10 @@ def main() -> None:
     ap.add_argument("--max-inner", type=int, default=20000,
                     help="inner steps per refinement step (smaller only for profiling captures)")
     ap.add_argument("--max-outer", type=int, default=12)
+    ap.add_argument("--projection", type=int, default=-1,
+                    help="start each solve from the A-norm best combination of u0 and the last "
+                         "K solutions (0: from u0; default 7 for the mixed solvers, 0 for FP64 "
+                         "CG)"),
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the other solvers' runs of the same timesteps")
     ap.add_argument("--skip-cpu", action="store_true")

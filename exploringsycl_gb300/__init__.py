@@ -41,14 +41,15 @@ class TLSolveStats(C.Structure):
 class TLSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("rel_tol", C.c_double), ("inner_tol", C.c_double),
                 ("max_inner", C.c_int), ("max_outer", C.c_int), ("stall_factor", C.c_double),
-                ("max_fallback", C.c_int), ("learned", C.c_void_p)]
+                ("max_fallback", C.c_int), ("learned", C.c_void_p), ("projection", C.c_int)]
 
 
 class TLSolveReport(C.Structure):
     _fields_ = [("outer_steps", C.c_int), ("inner_steps", C.c_int),
                 ("fallback_events", C.c_int), ("fallback_steps", C.c_int),
                 ("initial_rel_residual", C.c_double), ("final_rel_residual", C.c_double),
-                ("device_ms", C.c_float), ("inner_kernel_ms", C.c_float)]
+                ("device_ms", C.c_float), ("inner_kernel_ms", C.c_float),
+                ("projection_basis", C.c_int)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -105,6 +106,7 @@ SIGNATURES: dict[str, list] = {
     "tl_ppcg_inner_iteration": [_I, _I, _I, _D, _D, _D, _P, _P, _P, _P, _P],
     "tl_solve": [_I, _I, _I, _I, _D, _D, C.POINTER(TLSolveParams), _P, _P, _P, _P, _P, _P, _P,
                  _P, _P, C.POINTER(TLSolveReport)],
+    "tl_projection_reset": [],
 }
 
 # Entry points that do not take a context first.

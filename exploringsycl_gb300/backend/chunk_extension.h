@@ -27,6 +27,7 @@ typedef struct ChunkExtension {
   int replace_method;     /* -1, or a TL_METHOD_* that replaces the CG solve */
   double replace_rel_tol; /* its relative FP64 true-residual target */
   double replace_inner_tol;
+  int replace_projection; /* tl_solve_params.projection (gb300_projection) */
   struct tl_net* net;     /* the learned preconditioner (mixed-learned) */
   int fp64_fused;         /* 1: fused multiply-add contract of the FP64 CG */
 } ChunkExtension;

@@ -39,7 +39,9 @@
  * network's weights from `gb300_weights <file>` or TL_WEIGHTS: raw
  * little-endian FP32, tl_net_num_params() values), run_cg_init solves the timestep with
  * tl_solve to a relative FP64 true residual (`gb300_rel_tol`, default
- * 1e-10; `gb300_inner_tol`, default the method's own) and then reports rro = pw = 1,
+ * 1e-10; `gb300_inner_tol`, default the method's own; `gb300_projection K`,
+ * default 0, starts each solve from the A-norm best combination of u0 and
+ * the last K solutions instead of from u0) and then reports rro = pw = 1,
  * rrn = 0, so that the driver's CG loop ends after one pass and prints
  * "CG: 0 iterations"; the backend prints the true counts and the true
  * residual on a TL_SOLVE line. The reference driver ignores the gb300_* keys
@@ -130,16 +132,19 @@ static void read_backend_keys(Settings* settings, ChunkExtension* ext) {
   ext->replace_method = settings->preconditioner ? TL_METHOD_MIXED_JACOBI : -1;
   ext->replace_rel_tol = 1e-10;
   ext->replace_inner_tol = 0.0; /* the method's default */
+  ext->replace_projection = 0;  /* start each solve from u0, as the reference */
   ext->fp64_fused = 0;
   char weights[512] = "";
   FILE* f = fopen(settings->tea_in_filename, "r");
   if (f) {
     char line[512], word[128];
     double v;
+    int iv;
     while (fgets(line, sizeof(line), f)) {
       if (sscanf(line, " gb300_solver %127s", word) == 1) ext->replace_method = method_from_name(word);
       if (sscanf(line, " gb300_rel_tol %lf", &v) == 1) ext->replace_rel_tol = v;
       if (sscanf(line, " gb300_inner_tol %lf", &v) == 1) ext->replace_inner_tol = v;
+      if (sscanf(line, " gb300_projection %d", &iv) == 1) ext->replace_projection = iv;
       if (sscanf(line, " gb300_fp64 %127s", word) == 1) ext->fp64_fused = fp64_from_name(word);
       char path[512];
       if (sscanf(line, " gb300_weights %511s", path) == 1) snprintf(weights, sizeof(weights), "%s", path);
@@ -375,6 +380,7 @@ void run_cg_init(Chunk* chunk, Settings* settings, double rx, double ry,
     prm.learned = ext->net;
     prm.rel_tol = ext->replace_rel_tol;
     prm.inner_tol = ext->replace_inner_tol;
+    prm.projection = ext->replace_projection;
     prm.max_inner = settings->max_iters;
     prm.max_outer = 12;
     prm.stall_factor = 0.5;

@@ -118,18 +118,19 @@ class GpuChunk:
     def solve_timestep(self, method: str = "mixed", rel_tol: float = 1e-10,
                        inner_tol: float = 0.0, max_inner: int = 20000, max_outer: int = 12,
                        stall_factor: float = 0.5, max_fallback: int = 20000,
-                       learned=None) -> dict:
+                       learned=None, projection: int = 0) -> dict:
         """One timestep solved to a relative FP64 true residual with one of
         the solver-replacement methods (cg64 | mixed | mixed-jacobi |
-        mixed-learned | mixed-learned-layers, the last two with `learned`, a
-        learned.Net: its collapsed stencil in one persistent kernel, or the
-        network applied layer by layer)."""
+        mixed-learned | mixed-learned-coarse | mixed-learned-layers, the
+        learned ones with `learned`, a learned.Net). projection > 0 starts
+        from the A-norm best combination of u0 and up to that many solutions
+        of this chunk's earlier solves (0: from u0, as the reference)."""
         x, y, hd, f = self.x, self.y, self.hd, self.f
         rx, ry = self.rx_ry()
         self.halos(["energy", "density"], 2)
         prm = TLSolveParams(METHODS[method], rel_tol, inner_tol, max_inner, max_outer,
                             stall_factor, max_fallback,
-                            learned.h if learned is not None else None)
+                            learned.h if learned is not None else None, projection)
         rep = TLSolveReport()
         self.call("tl_solve", x, y, hd, self.coefficient, rx, ry, C.byref(prm), f["p"], f["r"],
                   f["u"], f["u0"], f["w"], f["kx"], f["ky"], f["density"], f["energy"],

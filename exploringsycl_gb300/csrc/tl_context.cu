@@ -91,6 +91,8 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_f32);
   cudaFree(ctx->d_ainv);
   cudaFree(ctx->d_ainv16);
+  cudaFree(ctx->d_proj);
+  cudaFree(ctx->d_proj_part);
   cudaFree(ctx->d_coarse_work);
   cudaFree(ctx->d_coarse_vec);
   cudaFree(ctx->d_hash);

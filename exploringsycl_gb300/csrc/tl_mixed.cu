@@ -8,7 +8,9 @@
  * The system is the reference's: A u = u0 with A the 5-point operator of
  * TeaLeaf/shared.h:59-63 built from kx, ky (TeaLeaf/c_kernels/sycl/cg.cpp:
  * 40-69), reflective (zero-flux) boundaries, initial guess u = u0 (the
- * reference's x0 = b, TeaLeaf/drivers/cg_driver.c:56-65). The stop rule is a
+ * reference's x0 = b, TeaLeaf/drivers/cg_driver.c:56-65), or with
+ * projection > 0 the A-norm best combination of u0 and the solutions of
+ * earlier solves with the same operator (tl_project.cu). The stop rule is a
  * relative FP64 *true* residual, ||u0 - A u||_2 <= rel_tol ||u0||_2 over the
  * interior, evaluated with the exact FP64 kernels.
  *
@@ -432,19 +434,80 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     return e;
   };
 
+  /* FP64 CG from the current u until the true residual meets the target:
+   * CG stops on its recursive residual, which can end a little below the
+   * true one, so up to two restarts from the true residual follow. Returns
+   * the final true residual norm in *rn. */
+  auto cg64_to_target = [&](int max_steps, int* steps_total, float* kernel_ms,
+                            double* rn) -> int {
+    double* uu1[1] = {u};
+    for (int round = 0; round < 3; ++round) {
+      int steps = 0;
+      int e = tl_internal_cg64_from_iterate(ctx, x, y, hd, target, max_steps - *steps_total, p,
+                                            r, u, u0, w, kx, ky, &steps);
+      if (e != TL_OK) return e;
+      *steps_total += steps;
+      *kernel_ms += ctx->last_solve.kernel_ms;
+      e = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu1, 1);
+      if (e != TL_OK) return e;
+      e = true_residual(rn);
+      if (e != TL_OK) return e;
+      if (*rn <= target || *steps_total >= max_steps || steps == 0) break;
+    }
+    return TL_OK;
+  };
+
+  /* Starting guess from the solutions of earlier solves with this operator
+   * (r holds the residual of u = u0 after the set-up); kept only while its
+   * true residual is below that of u = u0, rn_b. */
+  int basis = 0;
+  double rn_b = 0.0;
+  auto drop_guess = [&]() -> int {
+    basis = 0;
+    TL_CUDA(cudaMemcpyAsync(u, u0, (size_t)len * sizeof(double), cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+    return TL_OK;
+  };
+  if (prm->projection > 0) {
+    rc = norm2(ctx, x, y, hd, r, &rn_b);
+    if (rc != TL_OK) return rc;
+    rn_b = sqrt(rn_b);
+    rc = tl_internal_project_guess(ctx, prm->projection, x, y, hd, kx, ky, u0, r, u, &basis);
+    if (rc != TL_OK) return rc;
+  }
+
   if (prm->method == TL_METHOD_CG64) {
     int steps = 0;
-    /* r = 0 (a zero right-hand side) is solved already; CG would form 0/0. */
-    if (rro > 0.0) {
-      rc = tl_internal_cg64_loop(ctx, x, y, hd, target, prm->max_inner, p, r, u, w, kx, ky,
-                                 rro, nullptr, nullptr, &steps);
+    double* uu[1] = {u};
+    if (basis > 0) {
+      /* FP64 CG from the guess (or from u0 again if the guess is worse) */
+      double rn0 = 0.0;
+      rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu, 1);
       if (rc != TL_OK) return rc;
+      rc = true_residual(&rn0);
+      if (rc != TL_OK) return rc;
+      if (!(rn0 < rn_b)) {
+        rc = drop_guess();
+        if (rc != TL_OK) return rc;
+        rn0 = rn_b;
+      }
+      rep->initial_rel_residual = bnorm > 0 ? rn0 / bnorm : rn0;
+      double rn1 = 0.0;
+      rc = cg64_to_target(prm->max_inner, &steps, &rep->inner_kernel_ms, &rn1);
+      if (rc != TL_OK) return rc;
+    } else {
+      rep->initial_rel_residual = bnorm > 0 ? sqrt(rro) / bnorm : sqrt(rro);
+      /* r = 0 (a zero right-hand side) is solved already; CG would form 0/0. */
+      if (rro > 0.0) {
+        rc = tl_internal_cg64_loop(ctx, x, y, hd, target, prm->max_inner, p, r, u, w, kx, ky,
+                                   rro, nullptr, nullptr, &steps);
+        if (rc != TL_OK) return rc;
+      }
+      rep->inner_kernel_ms = rro > 0.0 ? ctx->last_solve.kernel_ms : 0.0f;
     }
     rep->inner_steps = steps;
     rep->outer_steps = 1;
-    rep->inner_kernel_ms = rro > 0.0 ? ctx->last_solve.kernel_ms : 0.0f;
     double rn = 0.0;
-    double* uu[1] = {u};
     rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu, 1);
     if (rc != TL_OK) return rc;
     rc = true_residual(&rn);
@@ -506,6 +569,14 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
       double rn = 0.0;
       rc = true_residual(&rn);
       if (rc != TL_OK) return rc;
+      if (outer == 0 && basis > 0 && !(rn < rn_b)) {
+        rc = drop_guess();
+        if (rc != TL_OK) return rc;
+        rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu, 1);
+        if (rc != TL_OK) return rc;
+        rc = true_residual(&rn);
+        if (rc != TL_OK) return rc;
+      }
       if (outer == 0) rep->initial_rel_residual = bnorm > 0 ? rn / bnorm : rn;
       rep->final_rel_residual = bnorm > 0 ? rn / bnorm : rn;
       if (rn <= target) break;
@@ -517,15 +588,9 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
          * the current iterate. */
         rep->fallback_events++;
         int steps = 0;
-        rc = tl_internal_cg64_from_iterate(ctx, x, y, hd, target, prm->max_fallback, p, r, u,
-                                           u0, w, kx, ky, &steps);
+        rc = cg64_to_target(prm->max_fallback, &steps, &rep->inner_kernel_ms, &rn);
         if (rc != TL_OK) return rc;
         rep->fallback_steps += steps;
-        rep->inner_kernel_ms += ctx->last_solve.kernel_ms;
-        rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, uu, 1);
-        if (rc != TL_OK) return rc;
-        rc = true_residual(&rn);
-        if (rc != TL_OK) return rc;
         rep->final_rel_residual = bnorm > 0 ? rn / bnorm : rn;
         break;
       }
@@ -621,6 +686,12 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     rc = tl_local_halos(ctx, x, y, hd, 1, 0xF, up, 2);
     if (rc != TL_OK) return rc;
   }
+  /* r is the true residual of the final u in both branches */
+  if (prm->projection > 0) {
+    rc = tl_internal_project_push(ctx, x, y, hd, u0, u, r);
+    if (rc != TL_OK) return rc;
+  }
+  rep->projection_basis = basis;
   TL_CUDA(cudaEventRecord(t1, ctx->stream));
   TL_CUDA(cudaEventSynchronize(t1));
   TL_CUDA(cudaEventElapsedTime(&ms_total, t0, t1));

@@ -243,7 +243,11 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
  * TeaLeaf/drivers/cg_driver.c:24). Each starts as the reference's
  * cg_init_driver (u = energy*density, kx, ky, halos, u0 = u) and solves
  * A u = u0 until ||u0 - A u||_2 <= rel_tol ||u0||_2 over the interior,
- * measured with the exact FP64 kernels. */
+ * measured with the exact FP64 kernels. TL_METHOD_CG64 from u0 stops as the
+ * reference's CG loop does, on its recurrence residual (sqrt(r.r) <= rel_tol
+ * ||u0||), so its true residual (final_rel_residual) can end a hair above;
+ * from a projected guess, and in every fall-back, FP64 CG restarts from the
+ * true residual until that meets the target. */
 #define TL_METHOD_CG64 0          /* exact FP64 CG (the drop-in kernel) */
 #define TL_METHOD_MIXED_CG 1      /* FP32 inner CG inside FP64 iterative refinement */
 #define TL_METHOD_MIXED_JACOBI 2  /* as above, Jacobi-preconditioned inner CG */
@@ -276,7 +280,17 @@ typedef struct tl_solve_params {
                            finishes the solve from the current iterate */
   int max_fallback;     /* FP64 CG steps allowed to the fall-back */
   struct tl_net* learned; /* TL_METHOD_MIXED_LEARNED: the network, else NULL */
+  int projection;       /* 0: start from u = u0, as the reference does. 1 ..
+                           TL_PROJ_MAX: keep the solutions of up to this many
+                           earlier solves with the same operator (kx, ky and
+                           the grid, checked by a content hash) in the
+                           context, and start from the A-norm best
+                           combination of u0 and them when its residual is
+                           smaller (successive right-hand sides; see
+                           tl_projection_reset) */
 } tl_solve_params;
+
+#define TL_PROJ_MAX 8
 
 typedef struct tl_solve_report {
   int outer_steps;
@@ -287,6 +301,7 @@ typedef struct tl_solve_report {
   double final_rel_residual;  /* ||u0 - A u|| / ||u0|| in FP64 at return */
   float device_ms;            /* whole solve, CUDA events on the context stream */
   float inner_kernel_ms;      /* the persistent inner / CG64 kernels alone */
+  int projection_basis;       /* directions of the starting guess (0: u0) */
 } tl_solve_report;
 
 int tl_solve(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
@@ -294,6 +309,9 @@ int tl_solve(tl_context* ctx, int x, int y, int halo_depth, int coefficient,
              double* r, double* u, double* u0, double* w, double* kx,
              double* ky, const double* density, const double* energy,
              tl_solve_report* report);
+/* Drops the solutions that tl_solve keeps for its starting guesses
+ * (tl_solve_params.projection): the next solve starts from u0. */
+int tl_projection_reset(tl_context* ctx);
 
 /* ----------------------------------------- learned preconditioner
  * M^-1 = D^-1 + S C^T C S: S = diag(D^-1/2) from the local operator diagonal, C four
