@@ -56,16 +56,17 @@ __device__ __forceinline__ bool interior(int kk, int jj, int x, int y, int hd) {
 
 /* The 5-point operator of TeaLeaf/shared.h:59-63 with the reference's
  * grouping: ((1 + (kx1+kx0)) + (ky1+ky0))*a - (kx1*a1 + kx0*a-1)
- * - (ky1*a+x + ky0*a-x). */
+ * - (ky1*a+x + ky0*a-x). The five products run on the integer pipes (the
+ * same IEEE products; these kernels are bound by the FP64 pipe). */
 template <class Load>
 __device__ __forceinline__ double smvp(Load a, const double* __restrict__ kx,
                                        const double* __restrict__ ky,
                                        unsigned i, int x) {
   const double kx0 = kx[i], kx1 = kx[i + 1];
   const double ky0 = ky[i], ky1 = ky[i + x];
-  return (1.0 + (kx1 + kx0) + (ky1 + ky0)) * a(i) -
-         (kx1 * a(i + 1) + kx0 * a(i - 1)) -
-         (ky1 * a(i + x) + ky0 * a(i - x));
+  return xmul<1>(1.0 + (kx1 + kx0) + (ky1 + ky0), a(i)) -
+         (xmul<1>(kx1, a(i + 1)) + xmul<1>(kx0, a(i - 1))) -
+         (xmul<1>(ky1, a(i + x)) + xmul<1>(ky0, a(i - x)));
 }
 
 struct PlainLoad {
@@ -283,6 +284,20 @@ struct ResidualOp {  /* TeaLeaf/c_kernels/sycl/solver_methods.cpp:34-65 */
       const double s = smvp(PlainLoad{u}, kx, ky, i, x);
       r[i] = u0[i] - s;
     }
+  }
+};
+
+/* calc_residual and calc_2norm of its result in one pass: the same r and
+ * the same sum (same cells, same tree) as ResidualOp then Norm2Op. */
+struct ResidualNormOp {
+  static constexpr int N = 1;
+  int x;
+  const double *u, *u0, *kx, *ky;
+  double* r;
+  __device__ void operator()(unsigned i, int, int, double* c) const {
+    const double rv = u0[i] - smvp(PlainLoad{u}, kx, ky, i, x);
+    r[i] = rv;
+    c[0] = rv * rv;
   }
 };
 
@@ -1145,6 +1160,13 @@ extern "C" int tl_copy_u(tl_context* ctx, int x, int y, int hd, const double* u,
   CTX_OK(ctx);
   DIMS_OK(x, y, hd);
   return launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
+}
+
+int tl_internal_residual_norm(tl_context* ctx, int x, int y, int hd, const double* u,
+                              const double* u0, double* r, const double* kx, const double* ky,
+                              double* rr) {
+  *rr = 0.0;
+  return launch_reduce(ctx, ResidualNormOp{x, u, u0, kx, ky, r}, x, y, hd, rr);
 }
 
 extern "C" int tl_calculate_residual(tl_context* ctx, int x, int y, int hd,

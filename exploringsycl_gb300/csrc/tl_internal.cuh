@@ -100,13 +100,14 @@ struct tl_context {
   unsigned long long* d_hash = nullptr;
   int coarse_H = 0, coarse_W = 0, coarse_blk = 0;
   unsigned long long coarse_hash = 0;
-  /* solutions of earlier solves with the same operator (tl_project.cu):
-   * proj_slots fields of proj_field_cap doubles, proj_count of them held,
-   * proj_order their slots from the oldest, proj_gram[i][j] = x_i . A x_j
-   * by slot, and the operator they belong to */
+  /* starting guesses of tl_solve (tl_project.cu): the newest solution X of
+   * the operator last seen (slot proj_xslot) and the differences of
+   * consecutive solutions before it (slots proj_order, oldest first), in
+   * proj_slots fields of proj_field_cap doubles, proj_count vectors held;
+   * proj_gram[i][j] = v_i . A v_j by slot; the operator they belong to */
   double* d_proj = nullptr;
   size_t proj_field_cap = 0;
-  int proj_slots = 0, proj_count = 0;
+  int proj_slots = 0, proj_count = 0, proj_xslot = 0;
   int proj_order[TL_PROJ_MAX] = {0};
   double proj_gram[TL_PROJ_MAX][TL_PROJ_MAX] = {{0.0}};
   double* d_proj_part = nullptr;  /* block partials of the dot products, then a hash word */
@@ -129,16 +130,23 @@ struct tl_coarse_level {
   float* ec;
 };
 
+/* r = u0 - A u over the interior (calc_residual) and r.r (calc_2norm of r)
+ * in one pass, both bit-identical to the two kernels (tl_fp64.cu). */
+int tl_internal_residual_norm(tl_context* ctx, int x, int y, int hd, const double* u,
+                              const double* u0, double* r, const double* kx, const double* ky,
+                              double* rr);
+
 /* Starting guess of tl_solve from the solutions of earlier solves with the
  * same operator (tl_project.cu): writes the guess into u's interior and the
- * number of basis directions kept into *basis (0: none, u untouched); r0 is
- * the residual of u = b. After the solve, push records the solution u with
- * its true residual r = b - A u. */
+ * number of basis directions kept into *basis (0: none, u untouched). After
+ * the solve, push records the solution u with its true residual
+ * r = b - A u. */
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
-                              const double* kx, const double* ky, const double* b,
-                              const double* r0, double* u, int* basis);
+                              const double* kx, const double* ky, const double* b, double* u,
+                              int* basis);
 int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double* b,
-                             const double* u, const double* r);
+                             const double* u, const double* r, const double* kx,
+                             const double* ky);
 
 /* Thread-local error message and helpers (tl_context.cu). */
 int tl_set_error(int code, const std::string& msg);

@@ -426,10 +426,8 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
   const double target = prm->rel_tol * bnorm;
 
   auto true_residual = [&](double* out) -> int {
-    int e = tl_calculate_residual(ctx, x, y, hd, u, u0, r, kx, ky);
-    if (e != TL_OK) return e;
     double rrv = 0.0;
-    e = norm2(ctx, x, y, hd, r, &rrv);
+    int e = tl_internal_residual_norm(ctx, x, y, hd, u, u0, r, kx, ky, &rrv);
     *out = sqrt(rrv);
     return e;
   };
@@ -457,9 +455,8 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     return TL_OK;
   };
 
-  /* Starting guess from the solutions of earlier solves with this operator
-   * (r holds the residual of u = u0 after the set-up); kept only while its
-   * true residual is below that of u = u0, rn_b. */
+  /* Starting guess from the solutions of earlier solves with this operator;
+   * kept only while its true residual is below that of u = u0, rn_b. */
   int basis = 0;
   double rn_b = 0.0;
   auto drop_guess = [&]() -> int {
@@ -469,10 +466,8 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
     return TL_OK;
   };
   if (prm->projection > 0) {
-    rc = norm2(ctx, x, y, hd, r, &rn_b);
-    if (rc != TL_OK) return rc;
-    rn_b = sqrt(rn_b);
-    rc = tl_internal_project_guess(ctx, prm->projection, x, y, hd, kx, ky, u0, r, u, &basis);
+    rn_b = sqrt(rro);  /* the set-up's r.p with p = r */
+    rc = tl_internal_project_guess(ctx, prm->projection, x, y, hd, kx, ky, u0, u, &basis);
     if (rc != TL_OK) return rc;
   }
 
@@ -688,7 +683,7 @@ extern "C" int tl_solve(tl_context* ctx, int x, int y, int hd, int coefficient, 
   }
   /* r is the true residual of the final u in both branches */
   if (prm->projection > 0) {
-    rc = tl_internal_project_push(ctx, x, y, hd, u0, u, r);
+    rc = tl_internal_project_push(ctx, x, y, hd, u0, u, r, kx, ky);
     if (rc != TL_OK) return rc;
   }
   rep->projection_basis = basis;

@@ -11,26 +11,35 @@
  * x0 = b. This is the projection method for successive right-hand sides of
  * P. F. Fischer, "Projection techniques for iterative solution of Ax = b
  * with successive right-hand sides", Comput. Methods Appl. Mech. Engrg. 163
- * (1998) 193-204, in the form that keeps the raw solutions and solves the
- * small Galerkin system each time:
+ * (1998) 193-204, in the form that solves the small Galerkin system each
+ * time:
  *
- *   V = [b, x_1 .. x_m] (x_j the held solutions), G = V^T A V, g = V^T b,
- *   x0 = V c with G c = g,
+ *   V a basis of span(x_1 .. x_m) (the last m solutions), G = V^T A V,
+ *   g = V^T b, x0 = V c with G c = g,
  *
- * which minimises ||x* - x0||_A over span(V). The solutions of consecutive
- * timesteps are nearly parallel (and b equals the newest one up to
- * rounding), so G is very ill-conditioned; the useful information sits in
- * directions whose eigenvalues are 1e-10 .. 1e-15 of the largest. G is
- * scaled to unit diagonal and solved by its eigen-decomposition (cyclic
- * Jacobi rotations, which resolve small eigenvalues of a scaled positive
- * definite matrix to high relative accuracy), dropping eigenvalues below
- * 1e-15 of the largest.
+ * which minimises ||x* - x0||_A over that span. In TeaLeaf b itself is the
+ * newest solution (u0 = energy * density, energy = u / density after the
+ * previous solve), so the span holds it up to rounding.
  *
- * No product with A is formed for the Gram matrix: A b = b - r0 with r0 the
- * residual of u = b that cg_init computes, and after the solve A u = b - r
- * with r the final true residual. Per solve this costs two passes of FP64
- * dot products (2m + 2 and 2m + 2 per cell, FP64-throughput bound on this
- * part) and one combination pass.
+ * Basis. The solutions of consecutive timesteps are nearly parallel; their
+ * own Gram matrix holds the directions that matter (the changes between
+ * timesteps, and the changes of those) only in its last digits, and in FP64
+ * at most 5 or 6 of 7 directions survive. The basis kept here is the newest
+ * solution X and the differences d_k = x_k - x_{k-1} of consecutive ones,
+ * each formed in FP64 from the full vectors, with its Gram matrix computed
+ * from them: the same span, with every direction resolved (7 of 7 in the
+ * CPU study that chose it, and a 10x smaller starting residual once the
+ * plain basis saturates). G is scaled to unit diagonal and solved by its
+ * eigen-decomposition (cyclic Jacobi rotations, which resolve small
+ * eigenvalues of a scaled positive definite matrix to high relative
+ * accuracy), dropping eigenvalues below 1e-15 of the largest.
+ *
+ * Cost per solve. Before: g (one FP64 dot product per basis vector, one
+ * pass) and x0 (one pass). After: one pass that forms d = u - X, applies A
+ * to it (the 5-point stencil on the difference) and its dot products with
+ * X, d and the kept differences; the new solution's Gram row follows from
+ * u = X + d (exact up to the rounding of d) as G[X][.] + G[d][.]. These
+ * passes are bound by GB300's FP64 rate, about 0.9 ms at 4096^2 in all.
  *
  * The held solutions belong to one operator: a 64-bit content hash of kx
  * and ky (and the grid's shape) is compared before each solve, and a
@@ -49,11 +58,16 @@
 namespace {
 
 constexpr int kDotThreads = 256;
-constexpr int kMaxVec = TL_PROJ_MAX + 1;  /* b and the held solutions */
+constexpr int kMaxVec = TL_PROJ_MAX;  /* basis vectors, and dot products of one pass */
 constexpr double kEigCut = 1e-15;
 
 struct VecList {
   const double* v[kMaxVec];
+};
+/* pairs (a_k, p_k) of the dot products of one pass */
+struct PairList {
+  const double* a[kMaxVec];
+  const double* p[kMaxVec];
 };
 struct CoefList {
   double c[kMaxVec];
@@ -85,47 +99,83 @@ __global__ void operator_hash_kernel(const double* __restrict__ kx, const double
   }
 }
 
-/* For each listed vector a_j (j < na): a_j . p and a_j . q over the
- * interior, into out[block][2 j + {0, 1}] (one FP64 partial per block,
- * summed in a fixed order inside the block; the host adds the blocks in
- * block order). */
-__global__ void __launch_bounds__(kDotThreads) proj_dots_kernel(int x, int y, int hd, VecList a,
-                                                                int na,
-                                                                const double* __restrict__ p,
-                                                                const double* __restrict__ q,
-                                                                double* out) {
-  __shared__ double s[kDotThreads / 32][2 * kMaxVec];
-  double acc[2 * kMaxVec];
+/* The dot products a_k . p_k (k < np) over the interior, into
+ * out[block][k] (one FP64 partial per block, summed in a fixed order inside
+ * the block; the host adds the blocks in block order). */
+__global__ void __launch_bounds__(kDotThreads) proj_dots_kernel(int x, int y, int hd, PairList L,
+                                                                int np, double* out) {
+  __shared__ double s[kDotThreads / 32][kMaxVec];
+  double acc[kMaxVec];
 #pragma unroll
-  for (int k = 0; k < 2 * kMaxVec; ++k) acc[k] = 0.0;
+  for (int k = 0; k < kMaxVec; ++k) acc[k] = 0.0;
   const int W = x - 2 * hd, H = y - 2 * hd;
   const size_t n = (size_t)W * H;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const size_t row = i / (size_t)W, col = i - row * (size_t)W;
     const size_t f = (row + hd) * (size_t)x + col + hd;
-    const double pv = p[f], qv = q[f];
 #pragma unroll
-    for (int j = 0; j < kMaxVec; ++j) {
-      if (j < na) {
-        const double av = a.v[j][f];
-        acc[2 * j] += av * pv;
-        acc[2 * j + 1] += av * qv;
-      }
-    }
+    for (int k = 0; k < kMaxVec; ++k)
+      if (k < np) acc[k] += L.a[k][f] * L.p[k][f];
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < 2 * kMaxVec; ++k) {
+  for (int k = 0; k < kMaxVec; ++k) {
     double v = acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) s[warp][k] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 2 * na) {
+  if (threadIdx.x < np) {
     double t = 0.0;
     for (int w = 0; w < kDotThreads / 32; ++w) t += s[w][threadIdx.x];
-    out[(size_t)blockIdx.x * 2 * na + threadIdx.x] = t;
+    out[(size_t)blockIdx.x * np + threadIdx.x] = t;
+  }
+}
+
+/* The pass after a solve with the held newest solution X: d = u - X over the
+ * interior into dnew; A d by the 5-point operator of TeaLeaf/shared.h:59-63
+ * applied to the difference (u and X carry the same reflective halos, so d's
+ * boundary fluxes vanish as u's do); and d . A d, X . A d and e_k . A d for
+ * the kept differences e_k, into out[block][0], [1] and [2 + k]. */
+__global__ void __launch_bounds__(kDotThreads)
+proj_push_kernel(int x, int y, int hd, const double* __restrict__ u, const double* __restrict__ X,
+                 const double* __restrict__ kx, const double* __restrict__ ky, VecList e, int ne,
+                 double* __restrict__ dnew, double* out) {
+  __shared__ double s[kDotThreads / 32][kMaxVec];
+  double acc[kMaxVec];
+#pragma unroll
+  for (int k = 0; k < kMaxVec; ++k) acc[k] = 0.0;
+  const int W = x - 2 * hd, H = y - 2 * hd;
+  const size_t n = (size_t)W * H;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = i / (size_t)W, col = i - row * (size_t)W;
+    const size_t f = (row + hd) * (size_t)x + col + hd;
+    const double d0 = u[f] - X[f];
+    const double kx0 = kx[f], kx1 = kx[f + 1], ky0 = ky[f], ky1 = ky[f + x];
+    const double ad = (1.0 + (kx1 + kx0) + (ky1 + ky0)) * d0 -
+                      (kx1 * (u[f + 1] - X[f + 1]) + kx0 * (u[f - 1] - X[f - 1])) -
+                      (ky1 * (u[f + x] - X[f + x]) + ky0 * (u[f - x] - X[f - x]));
+    dnew[f] = d0;
+    acc[0] += d0 * ad;
+    acc[1] += X[f] * ad;
+#pragma unroll
+    for (int k = 0; k + 2 < kMaxVec; ++k)
+      if (k < ne) acc[2 + k] += e.v[k][f] * ad;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kMaxVec; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 + ne) {
+    double t = 0.0;
+    for (int w = 0; w < kDotThreads / 32; ++w) t += s[w][threadIdx.x];
+    out[(size_t)blockIdx.x * (2 + ne) + threadIdx.x] = t;
   }
 }
 
@@ -190,30 +240,38 @@ void jacobi_eigen(int n, double* A, double* lam, double* V) {
 
 int grid_dots(const tl_context* ctx) { return 4 * ctx->num_sms; }
 
-/* Runs proj_dots_kernel and sums its block partials on the host in block
- * order: out[2 j + {0, 1}] = a_j . p, a_j . q. */
-int dots(tl_context* ctx, int x, int y, int hd, const VecList& a, int na, const double* p,
-         const double* q, double* out) {
+/* Sums the block partials of the last pass on the host in block order:
+ * out[k], k < np. */
+int sum_partials(tl_context* ctx, int np, double* out) {
   const int G = grid_dots(ctx);
-  proj_dots_kernel<<<G, kDotThreads, 0, ctx->stream>>>(x, y, hd, a, na, p, q, ctx->d_proj_part);
-  TL_CHECK_LAUNCH(ctx);
-  std::vector<double> h((size_t)G * 2 * na);
+  std::vector<double> h((size_t)G * np);
   TL_CUDA(cudaMemcpyAsync(h.data(), ctx->d_proj_part, h.size() * sizeof(double),
                           cudaMemcpyDeviceToHost, ctx->stream));
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
-  for (int k = 0; k < 2 * na; ++k) {
+  for (int k = 0; k < np; ++k) {
     double t = 0.0;
-    for (int g = 0; g < G; ++g) t += h[(size_t)g * 2 * na + k];
+    for (int g = 0; g < G; ++g) t += h[(size_t)g * np + k];
     out[k] = t;
   }
   return TL_OK;
 }
 
+int dots(tl_context* ctx, int x, int y, int hd, const PairList& L, int np, double* out) {
+  proj_dots_kernel<<<grid_dots(ctx), kDotThreads, 0, ctx->stream>>>(x, y, hd, L, np,
+                                                                    ctx->d_proj_part);
+  TL_CHECK_LAUNCH(ctx);
+  return sum_partials(ctx, np, out);
+}
+
+double* slot_ptr(tl_context* ctx, int slot) {
+  return ctx->d_proj + (size_t)slot * ctx->proj_field_cap;
+}
+
 }  // namespace
 
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
-                              const double* kx, const double* ky, const double* b,
-                              const double* r0, double* u, int* basis) {
+                              const double* kx, const double* ky, const double* b, double* u,
+                              int* basis) {
   *basis = 0;
   TL_REQUIRE(slots >= 1 && slots <= TL_PROJ_MAX, "tl_solve: projection must be 0 .. 8");
   const size_t len = (size_t)x * (size_t)y;
@@ -230,11 +288,11 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
   }
   if (!ctx->d_proj_part) {
     TL_CUDA(cudaMalloc(&ctx->d_proj_part,
-                       (size_t)grid_dots(ctx) * 2 * kMaxVec * sizeof(double) + 64));
+                       (size_t)grid_dots(ctx) * kMaxVec * sizeof(double) + 64));
   }
   /* the operator's identity */
   unsigned long long* d_hash = reinterpret_cast<unsigned long long*>(
-      ctx->d_proj_part + (size_t)grid_dots(ctx) * 2 * kMaxVec);
+      ctx->d_proj_part + (size_t)grid_dots(ctx) * kMaxVec);
   TL_CUDA(cudaMemsetAsync(d_hash, 0, sizeof(unsigned long long), ctx->stream));
   operator_hash_kernel<<<2 * ctx->num_sms, kDotThreads, 0, ctx->stream>>>(kx, ky, len, d_hash);
   TL_CHECK_LAUNCH(ctx);
@@ -248,25 +306,25 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
     ctx->proj_y = y;
     ctx->proj_hd = hd;
   }
-  const int m = ctx->proj_count;
-  if (m == 0) return TL_OK;
-  /* V = [b, held solutions from the oldest]; G[0][j] = v_j . A b =
-   * v_j . b - v_j . r0, g_j = v_j . b */
+  const int n = ctx->proj_count;
+  if (n == 0) return TL_OK;
+  /* V = [X, the differences from the oldest]; g_j = v_j . b */
+  int vslot[kMaxVec];
+  vslot[0] = ctx->proj_xslot;
+  for (int j = 1; j < n; ++j) vslot[j] = ctx->proj_order[j - 1];
   VecList V;
-  V.v[0] = b;
-  for (int j = 0; j < m; ++j) V.v[1 + j] = ctx->d_proj + (size_t)ctx->proj_order[j] * len;
-  const int n = m + 1;
-  double d[2 * kMaxVec];
-  int rc = dots(ctx, x, y, hd, V, n, b, r0, d);
-  if (rc != TL_OK) return rc;
-  double G[kMaxVec * kMaxVec], g[kMaxVec];
+  PairList L;
   for (int j = 0; j < n; ++j) {
-    g[j] = d[2 * j];
-    G[j] = G[j * n] = d[2 * j] - d[2 * j + 1];
+    V.v[j] = L.a[j] = slot_ptr(ctx, vslot[j]);
+    L.p[j] = b;
   }
-  for (int i = 0; i < m; ++i)
-    for (int j = 0; j < m; ++j)
-      G[(1 + i) * n + 1 + j] = ctx->proj_gram[ctx->proj_order[i]][ctx->proj_order[j]];
+  double g[kMaxVec];
+  int rc = dots(ctx, x, y, hd, L, n, g);
+  if (rc != TL_OK) return rc;
+  double G[kMaxVec * kMaxVec];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      G[i * n + j] = ctx->proj_gram[vslot[i]][vslot[j]];
   /* scale to unit diagonal, eigen-decompose, solve on the kept eigenvalues */
   double s[kMaxVec];
   for (int i = 0; i < n; ++i) {
@@ -301,34 +359,73 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
 }
 
 int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double* b,
-                             const double* u, const double* r) {
+                             const double* u, const double* r, const double* kx,
+                             const double* ky) {
   if (ctx->proj_slots < 1 || ctx->proj_x != x || ctx->proj_y != y || ctx->proj_hd != hd)
     return TL_OK;
   const size_t len = (size_t)x * (size_t)y;
-  /* the slot of the new solution: a free one, else the oldest */
-  const int full = ctx->proj_count == ctx->proj_slots;
-  const int slot = full ? ctx->proj_order[0] : ctx->proj_count;
-  const int keep = full ? ctx->proj_count - 1 : ctx->proj_count;
-  int order[TL_PROJ_MAX];
-  for (int j = 0; j < keep; ++j) order[j] = ctx->proj_order[j + (full ? 1 : 0)];
-  /* x_j . A u = x_j . b - x_j . r for the kept solutions and u itself */
-  VecList V;
-  for (int j = 0; j < keep; ++j) V.v[j] = ctx->d_proj + (size_t)order[j] * len;
-  V.v[keep] = u;
-  double d[2 * kMaxVec];
-  int rc = dots(ctx, x, y, hd, V, keep + 1, b, r, d);
-  if (rc != TL_OK) return rc;
-  for (int j = 0; j <= keep; ++j) {
-    const double v = d[2 * j] - d[2 * j + 1];
-    const int other = j < keep ? order[j] : slot;
-    ctx->proj_gram[slot][other] = v;
-    ctx->proj_gram[other][slot] = v;
+  auto (&G)[TL_PROJ_MAX][TL_PROJ_MAX] = ctx->proj_gram;
+  if (ctx->proj_count == 0 || ctx->proj_slots == 1) {
+    /* u becomes X: u . A u = u . b - u . r */
+    const int xs = ctx->proj_count == 0 ? 0 : ctx->proj_xslot;
+    PairList L;
+    L.a[0] = L.a[1] = u;
+    L.p[0] = b;
+    L.p[1] = r;
+    double d[2];
+    int rc = dots(ctx, x, y, hd, L, 2, d);
+    if (rc != TL_OK) return rc;
+    G[xs][xs] = d[0] - d[1];
+    TL_CUDA(cudaMemcpyAsync(slot_ptr(ctx, xs), u, len * sizeof(double),
+                            cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->proj_xslot = xs;
+    ctx->proj_count = 1;
+    return TL_OK;
   }
-  TL_CUDA(cudaMemcpyAsync(ctx->d_proj + (size_t)slot * len, u, len * sizeof(double),
-                          cudaMemcpyDeviceToDevice, ctx->stream));
-  order[keep] = slot;
-  for (int j = 0; j <= keep; ++j) ctx->proj_order[j] = order[j];
-  ctx->proj_count = keep + 1;
+  /* the new difference d = u - X goes to a free slot, else to the oldest
+   * difference's (dropped) */
+  const int xs = ctx->proj_xslot;
+  const int nd = ctx->proj_count - 1;
+  const bool full = ctx->proj_count == ctx->proj_slots;
+  int ds = -1;
+  if (full) {
+    ds = ctx->proj_order[0];
+  } else {
+    for (int c = 0; c < ctx->proj_slots && ds < 0; ++c) {
+      bool used = c == xs;
+      for (int j = 0; j < nd; ++j) used = used || ctx->proj_order[j] == c;
+      if (!used) ds = c;
+    }
+  }
+  const int first = full ? 1 : 0;
+  const int ne = nd - first;
+  int eslot[kMaxVec];
+  VecList E;
+  for (int k = 0; k < ne; ++k) {
+    eslot[k] = ctx->proj_order[first + k];
+    E.v[k] = slot_ptr(ctx, eslot[k]);
+  }
+  proj_push_kernel<<<grid_dots(ctx), kDotThreads, 0, ctx->stream>>>(
+      x, y, hd, u, slot_ptr(ctx, xs), kx, ky, E, ne, slot_ptr(ctx, ds), ctx->d_proj_part);
+  TL_CHECK_LAUNCH(ctx);
+  double d[kMaxVec];
+  int rc = sum_partials(ctx, 2 + ne, d);
+  if (rc != TL_OK) return rc;
+  const double dd = d[0], xd = d[1];
+  /* the new X = u = X + d: its row is X's plus d's */
+  for (int k = 0; k < ne; ++k) {
+    const double ue = G[xs][eslot[k]] + d[2 + k];
+    G[xs][eslot[k]] = G[eslot[k]][xs] = ue;
+    G[ds][eslot[k]] = G[eslot[k]][ds] = d[2 + k];
+  }
+  G[xs][xs] = G[xs][xs] + 2.0 * xd + dd;
+  G[xs][ds] = G[ds][xs] = xd + dd;
+  G[ds][ds] = dd;
+  TL_CUDA(cudaMemcpyAsync(slot_ptr(ctx, xs), u, len * sizeof(double), cudaMemcpyDeviceToDevice,
+                          ctx->stream));
+  for (int k = 0; k < ne; ++k) ctx->proj_order[k] = eslot[k];
+  ctx->proj_order[ne] = ds;
+  ctx->proj_count = ne + 2;
   return TL_OK;
 }
 

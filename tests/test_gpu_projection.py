@@ -1,8 +1,9 @@
 """Starting guesses from earlier solves with the same operator
 (tl_solve_params.projection, csrc/tl_project.cu) on the GPU.
 
-The guess is the A-norm best combination of u0 and the held solutions
-(Galerkin projection; P. F. Fischer 1998, successive right-hand sides). The
+The guess is the A-norm best combination of the held solutions (Galerkin
+projection; P. F. Fischer 1998, successive right-hand sides), kept as the
+newest solution and the differences of consecutive ones. The
 tests check: the solve still ends at the 1e-10 FP64 true residual with the
 same fields as a solve from u0; the guess's residual equals that of the same
 projection computed in float64 with numpy from the solutions the GPU
@@ -77,10 +78,11 @@ def test_projection_keeps_the_solution_and_cuts_the_steps(backend_built):
 
 
 def _galerkin_residual(b, held, kx, ky, cut=1e-15):
-    """||b - A x0|| / ||b|| for x0 = V c, V = [b, held...], (V^T A V) c = V^T b,
-    solved on the eigenvalues above cut x the largest of the unit-diagonal
-    scaling, in float64 with explicit products with A."""
-    V = [b] + held
+    """||b - A x0|| / ||b|| for x0 = V c with V = [the newest held solution,
+    the differences of consecutive ones] (the span of the held solutions),
+    (V^T A V) c = V^T b, solved on the eigenvalues above cut x the largest
+    of the unit-diagonal scaling, in float64 with explicit products with A."""
+    V = [held[-1]] + [held[i] - held[i - 1] for i in range(1, len(held))]
     AV = [_apply_a(v, kx, ky) for v in V]
     G = np.array([[np.vdot(vi, avj) for avj in AV] for vi in V])
     g = np.array([np.vdot(vi, b) for vi in V])
