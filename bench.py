@@ -114,7 +114,7 @@ NCU_BYTES_PER_CELL_STEP = {
     ("cg_persistent_kernel", "fused"): 115.0,      # profiles/cg_persistent_fp64_fused_4096.txt
     ("inner_cg_kernel", None): 51.3,               # profiles/inner_cg_mixed_jacobi_4096.txt
     ("lpcg_kernel", "mixed-learned"): 51.1,        # profiles/lpcg_learned_4096.txt
-    ("lpcg_kernel", "mixed-learned-coarse"): 55.7,  # profiles/lpcg_coarse_4096.txt
+    ("lpcg_kernel", "mixed-learned-coarse"): 53.5,  # profiles/lpcg_coarse_4096.txt
 }
 RANDOM_SEED = 1
 REL_TOL = 1e-10

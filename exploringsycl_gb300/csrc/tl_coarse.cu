@@ -200,7 +200,7 @@ int ensure(T** ptr, size_t* cap, size_t n, cudaStream_t stream) {
 }  // namespace
 
 int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, const float* ky,
-                               tl_coarse_level* out) {
+                               tl_coarse_level* out, const unsigned long long* known_hash) {
   const int sh = blk_shift_for(H, W);
   if (sh < 0) {
     return tl_set_error(TL_ERR_ARG,
@@ -214,14 +214,18 @@ int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, c
                   ctx->stream);
   if (rc != TL_OK) return rc;
   if (!ctx->d_hash) TL_CUDA(cudaMalloc(&ctx->d_hash, sizeof(unsigned long long)));
-  TL_CUDA(cudaMemsetAsync(ctx->d_hash, 0, sizeof(unsigned long long), ctx->stream));
-  const size_t n = (size_t)H * W;
-  coupling_hash_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(kx, ky, n, ctx->d_hash);
-  TL_CHECK_LAUNCH(ctx);
   unsigned long long hash = 0;
-  TL_CUDA(cudaMemcpyAsync(&hash, ctx->d_hash, sizeof(hash), cudaMemcpyDeviceToHost,
-                          ctx->stream));
-  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (known_hash) {
+    hash = *known_hash;
+  } else {
+    TL_CUDA(cudaMemsetAsync(ctx->d_hash, 0, sizeof(unsigned long long), ctx->stream));
+    const size_t n = (size_t)H * W;
+    coupling_hash_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(kx, ky, n, ctx->d_hash);
+    TL_CHECK_LAUNCH(ctx);
+    TL_CUDA(cudaMemcpyAsync(&hash, ctx->d_hash, sizeof(hash), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
   const bool cached = ctx->d_ainv && ctx->coarse_H == H && ctx->coarse_W == W &&
                       ctx->coarse_blk == (1 << sh) && ctx->coarse_hash == hash;
   if (!cached) {

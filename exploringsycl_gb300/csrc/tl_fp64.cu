@@ -1380,6 +1380,26 @@ int tl_internal_cg_setup(tl_context* ctx, int x, int y, int hd, int coefficient,
   return launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
 }
 
+/* The set-up of the solver-replacement path: cg_init_driver without
+ * cg_init_others (that path computes its own true residual): u =
+ * energy*density, kx, ky (skipped when the caller knows that they already
+ * hold this density's values), halos of u and p, u0 = u. */
+int tl_internal_cg_setup_lean(tl_context* ctx, int x, int y, int hd, int coefficient, double rx,
+                              double ry, double* p, double* r, double* u, double* u0, double* w,
+                              double* kx, double* ky, const double* density,
+                              const double* energy, bool couplings_current) {
+  int rc = launch_map(ctx, CgInitUOp{coefficient, p, r, u, w, density, energy, x, y}, x, y);
+  if (rc != TL_OK) return rc;
+  if (!couplings_current) {
+    rc = launch_map(ctx, CgInitKOp{x, y, hd, w, kx, ky, rx, ry}, x, y);
+    if (rc != TL_OK) return rc;
+  }
+  double* up[2] = {u, p};
+  rc = launch_halos(ctx, x, y, hd, 1, 0xF, up, 2);
+  if (rc != TL_OK) return rc;
+  return launch_map(ctx, CopyUOp{x, y, hd, u, u0}, x, y);
+}
+
 extern "C" int tl_cg_solve(tl_context* ctx, int x, int y, int hd, int coefficient,
                            double rx, double ry, double eps, int max_iters, double* p,
                            double* r, double* u, double* u0, double* w, double* kx,

@@ -110,8 +110,21 @@ struct tl_context {
   int proj_slots = 0, proj_count = 0, proj_xslot = 0;
   int proj_order[TL_PROJ_MAX] = {0};
   double proj_gram[TL_PROJ_MAX][TL_PROJ_MAX] = {{0.0}};
-  double* d_proj_part = nullptr;  /* block partials of the dot products, then a hash word */
+  double* d_proj_part = nullptr;  /* block partials of the dot products */
   int proj_x = 0, proj_y = 0, proj_hd = 0;
+  int proj_last_n = 0;            /* the last guess: its basis slots and coefficients */
+  int proj_last_slot[TL_PROJ_MAX] = {0};
+  double proj_last_coef[TL_PROJ_MAX] = {0.0};
+  /* the operator tl_solve's replacement path saw last: x, y, hd, the hash of
+   * density with rx, ry and the coefficient kind, and the hash of the kx,
+   * ky it computed from them (cg_init's couplings are recomputed only when
+   * one of them changed); the FP32 coefficients packed from that operator
+   * (packed_kind 1: the learned solvers' packed layout, 2: the halo layout) */
+  int op_x = 0, op_y = 0, op_hd = 0;
+  unsigned long long op_dens_hash = 0, op_k_hash = 0;
+  int packed_kind = 0;
+  unsigned long long packed_hash = 0;
+  unsigned long long* d_hash64 = nullptr;
   unsigned long long proj_hash = 0;
 };
 
@@ -130,6 +143,19 @@ struct tl_coarse_level {
   float* ec;
 };
 
+/* Set-up of tl_solve's replacement path (tl_fp64.cu): cg_init_driver
+ * without cg_init_others; kx, ky are left as they are when
+ * couplings_current. */
+int tl_internal_cg_setup_lean(tl_context* ctx, int x, int y, int hd, int coefficient, double rx,
+                              double ry, double* p, double* r, double* u, double* u0, double* w,
+                              double* kx, double* ky, const double* density,
+                              const double* energy, bool couplings_current);
+
+/* 64-bit content hash of the n doubles of a (and of b, when not NULL),
+ * order-independent, mixed with salt (tl_project.cu). */
+int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, size_t n,
+                       unsigned long long salt, unsigned long long* out);
+
 /* r = u0 - A u over the interior (calc_residual) and r.r (calc_2norm of r)
  * in one pass, both bit-identical to the two kernels (tl_fp64.cu). */
 int tl_internal_residual_norm(tl_context* ctx, int x, int y, int hd, const double* u,
@@ -142,8 +168,10 @@ int tl_internal_residual_norm(tl_context* ctx, int x, int y, int hd, const doubl
  * the solve, push records the solution u with its true residual
  * r = b - A u. */
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
-                              const double* kx, const double* ky, const double* b, double* u,
+                              unsigned long long op_hash, const double* b, double* u,
                               int* basis);
+/* Writes the last guess into u again (after u was overwritten). */
+int tl_internal_project_recombine(tl_context* ctx, int x, int y, int hd, double* u);
 int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double* b,
                              const double* u, const double* r, const double* kx,
                              const double* ky);
@@ -181,9 +209,11 @@ int tl_internal_fpcg_collapsed(tl_context* ctx, const void* umma, const float* k
                                float* pb, double tol, int max_iters, int* iters,
                                double* rr_final, const tl_coarse_level* coarse = nullptr);
 /* The coarse level for the couplings kx, ky of a packed [H][W] field
- * (tl_coarse.cu): rebuilt only when H, W or the couplings change. */
+ * (tl_coarse.cu): rebuilt only when H, W or the couplings change. A caller
+ * that knows a content hash of the couplings passes it in known_hash (the
+ * coarse level then skips its own). */
 int tl_internal_coarse_prepare(tl_context* ctx, int H, int W, const float* kx, const float* ky,
-                               tl_coarse_level* out);
+                               tl_coarse_level* out, const unsigned long long* known_hash = nullptr);
 int tl_internal_cg64_from_iterate(tl_context* ctx, int x, int y, int hd, double eps,
                                   int max_iters, double* p, double* r, double* u,
                                   const double* u0, double* w, const double* kx,

@@ -73,17 +73,17 @@ struct CoefList {
   double c[kMaxVec];
 };
 
-/* Order-independent 64-bit hash of the operator's couplings (all x*y words
- * of kx and ky, halos included: cg_init writes them deterministically). */
-__global__ void operator_hash_kernel(const double* __restrict__ kx, const double* __restrict__ ky,
-                                     size_t n, unsigned long long* out) {
+/* Order-independent 64-bit hash of the n doubles of a (and b when not
+ * NULL): a wrapping sum of the mixed words and their indices. */
+__global__ void hash64_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                              size_t n, unsigned long long* out) {
   __shared__ unsigned long long s[kDotThreads / 32];
   unsigned long long h = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    unsigned long long a = (unsigned long long)__double_as_longlong(kx[i]);
-    unsigned long long b = (unsigned long long)__double_as_longlong(ky[i]);
-    unsigned long long v = a ^ (b * 0xD6E8FEB86659FD93ull) ^ ((unsigned long long)i * 0x9E3779B97F4A7C15ull);
+    unsigned long long v = (unsigned long long)__double_as_longlong(a[i]);
+    if (b) v ^= (unsigned long long)__double_as_longlong(b[i]) * 0xD6E8FEB86659FD93ull;
+    v ^= (unsigned long long)i * 0x9E3779B97F4A7C15ull;
     v ^= v >> 32;
     v *= 0xBF58476D1CE4E5B9ull;
     v ^= v >> 29;
@@ -270,7 +270,7 @@ double* slot_ptr(tl_context* ctx, int slot) {
 }  // namespace
 
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
-                              const double* kx, const double* ky, const double* b, double* u,
+                              unsigned long long op_hash, const double* b, double* u,
                               int* basis) {
   *basis = 0;
   TL_REQUIRE(slots >= 1 && slots <= TL_PROJ_MAX, "tl_solve: projection must be 0 .. 8");
@@ -287,25 +287,17 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
     ctx->proj_field_cap = len;
   }
   if (!ctx->d_proj_part) {
-    TL_CUDA(cudaMalloc(&ctx->d_proj_part,
-                       (size_t)grid_dots(ctx) * kMaxVec * sizeof(double) + 64));
+    TL_CUDA(cudaMalloc(&ctx->d_proj_part, (size_t)grid_dots(ctx) * kMaxVec * sizeof(double)));
   }
   /* the operator's identity */
-  unsigned long long* d_hash = reinterpret_cast<unsigned long long*>(
-      ctx->d_proj_part + (size_t)grid_dots(ctx) * kMaxVec);
-  TL_CUDA(cudaMemsetAsync(d_hash, 0, sizeof(unsigned long long), ctx->stream));
-  operator_hash_kernel<<<2 * ctx->num_sms, kDotThreads, 0, ctx->stream>>>(kx, ky, len, d_hash);
-  TL_CHECK_LAUNCH(ctx);
-  unsigned long long hash = 0;
-  TL_CUDA(cudaMemcpyAsync(&hash, d_hash, sizeof(hash), cudaMemcpyDeviceToHost, ctx->stream));
-  TL_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (hash != ctx->proj_hash || x != ctx->proj_x || y != ctx->proj_y || hd != ctx->proj_hd) {
+  if (op_hash != ctx->proj_hash || x != ctx->proj_x || y != ctx->proj_y || hd != ctx->proj_hd) {
     ctx->proj_count = 0;
-    ctx->proj_hash = hash;
+    ctx->proj_hash = op_hash;
     ctx->proj_x = x;
     ctx->proj_y = y;
     ctx->proj_hd = hd;
   }
+  ctx->proj_last_n = 0;
   const int n = ctx->proj_count;
   if (n == 0) return TL_OK;
   /* V = [X, the differences from the oldest]; g_j = v_j . b */
@@ -354,7 +346,43 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
   }
   proj_combine_kernel<<<4 * ctx->num_sms, 256, 0, ctx->stream>>>(x, y, hd, V, c, n, u);
   TL_CHECK_LAUNCH(ctx);
+  ctx->proj_last_n = n;
+  for (int i = 0; i < n; ++i) {
+    ctx->proj_last_slot[i] = vslot[i];
+    ctx->proj_last_coef[i] = c.c[i];
+  }
   *basis = kept;
+  return TL_OK;
+}
+
+int tl_internal_project_recombine(tl_context* ctx, int x, int y, int hd, double* u) {
+  const int n = ctx->proj_last_n;
+  TL_REQUIRE(n > 0, "tl_solve: no projected guess to restore");
+  VecList V;
+  CoefList c;
+  for (int i = 0; i < kMaxVec; ++i) c.c[i] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    V.v[i] = slot_ptr(ctx, ctx->proj_last_slot[i]);
+    c.c[i] = ctx->proj_last_coef[i];
+  }
+  proj_combine_kernel<<<4 * ctx->num_sms, 256, 0, ctx->stream>>>(x, y, hd, V, c, n, u);
+  TL_CHECK_LAUNCH(ctx);
+  return TL_OK;
+}
+
+int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, size_t n,
+                       unsigned long long salt, unsigned long long* out) {
+  if (!ctx->d_hash64) TL_CUDA(cudaMalloc(&ctx->d_hash64, sizeof(unsigned long long)));
+  TL_CUDA(cudaMemsetAsync(ctx->d_hash64, 0, sizeof(unsigned long long), ctx->stream));
+  hash64_kernel<<<2 * ctx->num_sms, kDotThreads, 0, ctx->stream>>>(a, b, n, ctx->d_hash64);
+  TL_CHECK_LAUNCH(ctx);
+  unsigned long long h = 0;
+  TL_CUDA(cudaMemcpyAsync(&h, ctx->d_hash64, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  TL_CUDA(cudaStreamSynchronize(ctx->stream));
+  h ^= salt;
+  h *= 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  *out = h;
   return TL_OK;
 }
 

@@ -184,3 +184,31 @@ def test_projection_above_the_limit_is_refused(backend_built):
             g.solve_timestep("mixed", rel_tol=1e-10, projection=9)
     finally:
         g.close()
+
+
+def test_set_up_couplings_follow_density_and_overwrites(backend_built):
+    """The replacement path computes kx, ky again only when density (with
+    rx, ry, the coefficient kind) or kx, ky themselves changed: after a
+    change of density, and after kx is overwritten between solves, the
+    couplings equal those of a fresh chunk."""
+    from exploringsycl_gb300.chunk import GpuChunk
+    d = dk.random_deck(128, seed=49, end_step=6, initial_timestep=0.004 * 1024)
+    a, b = GpuChunk(d), GpuChunk(d)
+    try:
+        for _ in range(2):
+            a.solve_timestep("mixed", rel_tol=1e-10, projection=3)
+        dens = 2.0 * a.read("density")
+        a.ctx.upload(a.f["density"], dens)
+        b.ctx.upload(b.f["density"], dens)
+        ra = a.solve_timestep("mixed", rel_tol=1e-10, projection=3)
+        b.solve_timestep("mixed", rel_tol=1e-10, projection=3)
+        for name in ("kx", "ky"):
+            assert np.array_equal(_interior(a, name), _interior(b, name)), name
+        assert ra["final_rel_residual"] <= 1e-10
+        a.ctx.upload(a.f["kx"], np.zeros(a.n))
+        ra = a.solve_timestep("mixed", rel_tol=1e-10, projection=3)
+        assert np.array_equal(_interior(a, "kx"), _interior(b, "kx"))
+        assert ra["final_rel_residual"] <= 1e-10
+    finally:
+        a.close()
+        b.close()
