@@ -94,6 +94,7 @@ extern "C" int tl_context_destroy(tl_context* ctx) {
   cudaFree(ctx->d_proj);
   cudaFree(ctx->d_proj_part);
   cudaFree(ctx->d_hash64);
+  cudaFree(ctx->d_diag64);
   cudaFree(ctx->d_coarse_work);
   cudaFree(ctx->d_coarse_vec);
   cudaFree(ctx->d_hash);

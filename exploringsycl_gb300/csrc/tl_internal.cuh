@@ -125,6 +125,10 @@ struct tl_context {
   int packed_kind = 0;
   unsigned long long packed_hash = 0;
   unsigned long long* d_hash64 = nullptr;
+  /* the diagonal of that operator (FP64, x*y), for the replacement path */
+  double* d_diag64 = nullptr;
+  size_t diag64_cap = 0;
+  unsigned long long diag64_id = 0;
   unsigned long long proj_hash = 0;
 };
 
@@ -151,10 +155,12 @@ int tl_internal_cg_setup_lean(tl_context* ctx, int x, int y, int hd, int coeffic
                               double* kx, double* ky, const double* density,
                               const double* energy, bool couplings_current);
 
-/* 64-bit content hash of the n doubles of a (and of b, when not NULL),
- * order-independent, mixed with salt (tl_project.cu). */
-int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, size_t n,
-                       unsigned long long salt, unsigned long long* out);
+/* 64-bit content hashes of n doubles in one pass (tl_project.cu): *out_a
+ * of a (mixed with salt_a; a may be NULL), *out_bc of b and c together (c
+ * may be NULL; b NULL leaves *out_bc alone). */
+int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, const double* c,
+                       size_t n, unsigned long long salt_a, unsigned long long* out_a,
+                       unsigned long long* out_bc);
 
 /* r = u0 - A u over the interior (calc_residual) and r.r (calc_2norm of r)
  * in one pass, both bit-identical to the two kernels (tl_fp64.cu). */
@@ -164,17 +170,19 @@ int tl_internal_residual_norm(tl_context* ctx, int x, int y, int hd, const doubl
 
 /* Starting guess of tl_solve from the solutions of earlier solves with the
  * same operator (tl_project.cu): writes the guess into u's interior and the
- * number of basis directions kept into *basis (0: none, u untouched). After
+ * number of basis directions kept into *basis (0: none, u untouched); *bb
+ * receives b.b when solutions were held (the pass that sums them), and is
+ * left alone otherwise. After
  * the solve, push records the solution u with its true residual
  * r = b - A u. */
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
                               unsigned long long op_hash, const double* b, double* u,
-                              int* basis);
+                              int* basis, double* bb);
 /* Writes the last guess into u again (after u was overwritten). */
 int tl_internal_project_recombine(tl_context* ctx, int x, int y, int hd, double* u);
 int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double* b,
                              const double* u, const double* r, const double* kx,
-                             const double* ky);
+                             const double* ky, const double* diag);
 
 /* Thread-local error message and helpers (tl_context.cu). */
 int tl_set_error(int code, const std::string& msg);

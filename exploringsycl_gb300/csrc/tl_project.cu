@@ -35,7 +35,7 @@
  * accuracy), dropping eigenvalues below 1e-15 of the largest.
  *
  * Cost per solve. Before: g (one FP64 dot product per basis vector, one
- * pass) and x0 (one pass). After: one pass that forms d = u - X, applies A
+ * pass that also sums b.b for the solve's stop rule) and x0 (one pass). After: one pass that forms d = u - X, applies A
  * to it (the 5-point stencil on the difference) and its dot products with
  * X, d and the kept differences; the new solution's Gram row follows from
  * u = X + d (exact up to the rounding of d) as G[X][.] + G[d][.]. These
@@ -58,7 +58,7 @@
 namespace {
 
 constexpr int kDotThreads = 256;
-constexpr int kMaxVec = TL_PROJ_MAX;  /* basis vectors, and dot products of one pass */
+constexpr int kMaxVec = TL_PROJ_MAX + 1;  /* dot products of one pass, at most */
 constexpr double kEigCut = 1e-15;
 
 struct VecList {
@@ -73,29 +73,52 @@ struct CoefList {
   double c[kMaxVec];
 };
 
-/* Order-independent 64-bit hash of the n doubles of a (and b when not
- * NULL): a wrapping sum of the mixed words and their indices. */
+/* Order-independent 64-bit hashes of n doubles: out[0] of a, out[1] of b
+ * and c together (a or c may be NULL; b NULL skips out[1]). Each 32-bit half of
+ * each double is mixed with its position (multiply, xorshift) and the mixed
+ * words are summed modulo 2^64: any change of a word changes the sum unless
+ * another change cancels it exactly. */
+__device__ __forceinline__ unsigned long long mix32(unsigned w, unsigned pos) {
+  w ^= pos * 0x9E3779B9u;
+  w *= 0x85EBCA6Bu;
+  w ^= w >> 13;
+  w *= 0xC2B2AE35u;
+  return (unsigned long long)w << (pos & 31u);
+}
+
 __global__ void hash64_kernel(const double* __restrict__ a, const double* __restrict__ b,
-                              size_t n, unsigned long long* out) {
-  __shared__ unsigned long long s[kDotThreads / 32];
-  unsigned long long h = 0;
+                              const double* __restrict__ c, size_t n, unsigned long long* out) {
+  __shared__ unsigned long long s[2][kDotThreads / 32];
+  unsigned long long ha = 0, hb = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    unsigned long long v = (unsigned long long)__double_as_longlong(a[i]);
-    if (b) v ^= (unsigned long long)__double_as_longlong(b[i]) * 0xD6E8FEB86659FD93ull;
-    v ^= (unsigned long long)i * 0x9E3779B97F4A7C15ull;
-    v ^= v >> 32;
-    v *= 0xBF58476D1CE4E5B9ull;
-    v ^= v >> 29;
-    h += v;
+    const unsigned p = 4u * (unsigned)i;
+    if (a) {
+      const unsigned long long va = (unsigned long long)__double_as_longlong(a[i]);
+      ha += mix32((unsigned)va, p) + mix32((unsigned)(va >> 32), p + 1u);
+    }
+    if (b) {
+      const unsigned long long vb = (unsigned long long)__double_as_longlong(b[i]);
+      hb += mix32((unsigned)vb, p) + mix32((unsigned)(vb >> 32), p + 1u);
+      if (c) {
+        const unsigned long long vc = (unsigned long long)__double_as_longlong(c[i]);
+        hb += mix32((unsigned)vc, p + 2u) + mix32((unsigned)(vc >> 32), p + 3u);
+      }
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = h;
+  for (int o = 16; o > 0; o >>= 1) {
+    ha += __shfl_xor_sync(0xffffffffu, ha, o);
+    hb += __shfl_xor_sync(0xffffffffu, hb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s[0][threadIdx.x >> 5] = ha;
+    s[1][threadIdx.x >> 5] = hb;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 2) {
     unsigned long long t = 0;
-    for (int w = 0; w < kDotThreads / 32; ++w) t += s[w];
-    atomicAdd(out, t);
+    for (int w = 0; w < kDotThreads / 32; ++w) t += s[threadIdx.x][w];
+    atomicAdd(out + threadIdx.x, t);
   }
 }
 
@@ -135,13 +158,14 @@ __global__ void __launch_bounds__(kDotThreads) proj_dots_kernel(int x, int y, in
 
 /* The pass after a solve with the held newest solution X: d = u - X over the
  * interior into dnew; A d by the 5-point operator of TeaLeaf/shared.h:59-63
- * applied to the difference (u and X carry the same reflective halos, so d's
+ * (its diagonal precomputed, fused multiply-adds) applied to the difference (u and X carry the same reflective halos, so d's
  * boundary fluxes vanish as u's do); and d . A d, X . A d and e_k . A d for
  * the kept differences e_k, into out[block][0], [1] and [2 + k]. */
 __global__ void __launch_bounds__(kDotThreads)
 proj_push_kernel(int x, int y, int hd, const double* __restrict__ u, const double* __restrict__ X,
-                 const double* __restrict__ kx, const double* __restrict__ ky, VecList e, int ne,
-                 double* __restrict__ dnew, double* out) {
+                 const double* __restrict__ kx, const double* __restrict__ ky,
+                 const double* __restrict__ diag, VecList e, int ne, double* __restrict__ dnew,
+                 double* out) {
   __shared__ double s[kDotThreads / 32][kMaxVec];
   double acc[kMaxVec];
 #pragma unroll
@@ -153,10 +177,11 @@ proj_push_kernel(int x, int y, int hd, const double* __restrict__ u, const doubl
     const size_t row = i / (size_t)W, col = i - row * (size_t)W;
     const size_t f = (row + hd) * (size_t)x + col + hd;
     const double d0 = u[f] - X[f];
-    const double kx0 = kx[f], kx1 = kx[f + 1], ky0 = ky[f], ky1 = ky[f + x];
-    const double ad = (1.0 + (kx1 + kx0) + (ky1 + ky0)) * d0 -
-                      (kx1 * (u[f + 1] - X[f + 1]) + kx0 * (u[f - 1] - X[f - 1])) -
-                      (ky1 * (u[f + x] - X[f + x]) + ky0 * (u[f - x] - X[f - x]));
+    double ad = diag[f] * d0;
+    ad = fma(-ky[f], u[f - x] - X[f - x], ad);
+    ad = fma(-ky[f + x], u[f + x] - X[f + x], ad);
+    ad = fma(-kx[f], u[f - 1] - X[f - 1], ad);
+    ad = fma(-kx[f + 1], u[f + 1] - X[f + 1], ad);
     dnew[f] = d0;
     acc[0] += d0 * ad;
     acc[1] += X[f] * ad;
@@ -271,7 +296,7 @@ double* slot_ptr(tl_context* ctx, int slot) {
 
 int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
                               unsigned long long op_hash, const double* b, double* u,
-                              int* basis) {
+                              int* basis, double* bb) {
   *basis = 0;
   TL_REQUIRE(slots >= 1 && slots <= TL_PROJ_MAX, "tl_solve: projection must be 0 .. 8");
   const size_t len = (size_t)x * (size_t)y;
@@ -310,9 +335,11 @@ int tl_internal_project_guess(tl_context* ctx, int slots, int x, int y, int hd,
     V.v[j] = L.a[j] = slot_ptr(ctx, vslot[j]);
     L.p[j] = b;
   }
+  L.a[n] = L.p[n] = b;
   double g[kMaxVec];
-  int rc = dots(ctx, x, y, hd, L, n, g);
+  int rc = dots(ctx, x, y, hd, L, n + 1, g);
   if (rc != TL_OK) return rc;
+  *bb = g[n];
   double G[kMaxVec * kMaxVec];
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j)
@@ -370,25 +397,30 @@ int tl_internal_project_recombine(tl_context* ctx, int x, int y, int hd, double*
   return TL_OK;
 }
 
-int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, size_t n,
-                       unsigned long long salt, unsigned long long* out) {
-  if (!ctx->d_hash64) TL_CUDA(cudaMalloc(&ctx->d_hash64, sizeof(unsigned long long)));
-  TL_CUDA(cudaMemsetAsync(ctx->d_hash64, 0, sizeof(unsigned long long), ctx->stream));
-  hash64_kernel<<<2 * ctx->num_sms, kDotThreads, 0, ctx->stream>>>(a, b, n, ctx->d_hash64);
+int tl_internal_hash64(tl_context* ctx, const double* a, const double* b, const double* c,
+                       size_t n, unsigned long long salt_a, unsigned long long* out_a,
+                       unsigned long long* out_bc) {
+  if (!ctx->d_hash64) TL_CUDA(cudaMalloc(&ctx->d_hash64, 2 * sizeof(unsigned long long)));
+  TL_CUDA(cudaMemsetAsync(ctx->d_hash64, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  hash64_kernel<<<8 * ctx->num_sms, kDotThreads, 0, ctx->stream>>>(a, b, c, n, ctx->d_hash64);
   TL_CHECK_LAUNCH(ctx);
-  unsigned long long h = 0;
-  TL_CUDA(cudaMemcpyAsync(&h, ctx->d_hash64, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned long long h[2] = {0, 0};
+  TL_CUDA(cudaMemcpyAsync(h, ctx->d_hash64, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   TL_CUDA(cudaStreamSynchronize(ctx->stream));
-  h ^= salt;
-  h *= 0x94D049BB133111EBull;
-  h ^= h >> 31;
-  *out = h;
+  auto fin = [](unsigned long long v, unsigned long long salt) {
+    v ^= salt;
+    v *= 0x94D049BB133111EBull;
+    v ^= v >> 31;
+    return v;
+  };
+  if (out_a) *out_a = fin(h[0], salt_a);
+  if (out_bc) *out_bc = fin(h[1], 0);
   return TL_OK;
 }
 
 int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double* b,
                              const double* u, const double* r, const double* kx,
-                             const double* ky) {
+                             const double* ky, const double* diag) {
   if (ctx->proj_slots < 1 || ctx->proj_x != x || ctx->proj_y != y || ctx->proj_hd != hd)
     return TL_OK;
   const size_t len = (size_t)x * (size_t)y;
@@ -434,7 +466,7 @@ int tl_internal_project_push(tl_context* ctx, int x, int y, int hd, const double
     E.v[k] = slot_ptr(ctx, eslot[k]);
   }
   proj_push_kernel<<<grid_dots(ctx), kDotThreads, 0, ctx->stream>>>(
-      x, y, hd, u, slot_ptr(ctx, xs), kx, ky, E, ne, slot_ptr(ctx, ds), ctx->d_proj_part);
+      x, y, hd, u, slot_ptr(ctx, xs), kx, ky, diag, E, ne, slot_ptr(ctx, ds), ctx->d_proj_part);
   TL_CHECK_LAUNCH(ctx);
   double d[kMaxVec];
   int rc = sum_partials(ctx, 2 + ne, d);

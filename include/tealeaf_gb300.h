@@ -243,7 +243,9 @@ int tl_cg_solve(tl_context* ctx, int x, int y, int halo_depth,
  * TeaLeaf/drivers/cg_driver.c:24). Each starts as the reference's
  * cg_init_driver (u = energy*density, kx, ky, halos, u0 = u) and solves
  * A u = u0 until ||u0 - A u||_2 <= rel_tol ||u0||_2 over the interior,
- * measured with the exact FP64 kernels. TL_METHOD_CG64 from u0 stops as the
+ * measured in FP64 (with the reference's residual kernel for TL_METHOD_CG64
+ * from u0; the other paths evaluate the same operator with fused
+ * multiply-adds on its precomputed diagonal). TL_METHOD_CG64 from u0 stops as the
  * reference's CG loop does, on its recurrence residual (sqrt(r.r) <= rel_tol
  * ||u0||), so its true residual (final_rel_residual) can end a hair above;
  * from a projected guess, and in every fall-back, FP64 CG restarts from the
