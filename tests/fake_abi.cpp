@@ -308,9 +308,11 @@ int tl_ppcg_inner_iteration(tl_context*, int, int, int, double, double, double, 
 int tl_solve(tl_context*, int, int, int, int, double, double, const tl_solve_params* prm,
              double*, double*, double*, double*, double*, double*, double*, const double*,
              const double*, tl_solve_report* rep) {
-  FAKE_CALL("tl_solve", "tl_solve method=%d rel_tol=%.17g inner_tol=%.17g max_inner=%d learned=%d",
-            prm->method, prm->rel_tol, prm->inner_tol, prm->max_inner,
-            prm->learned != nullptr);
+  FAKE_CALL("tl_solve",
+            "tl_solve method=%d rel_tol=%.17g inner_tol=%.17g max_inner=%d learned=%d "
+            "projection=%d",
+            prm->method, prm->rel_tol, prm->inner_tol, prm->max_inner, prm->learned != nullptr,
+            prm->projection);
   memset(rep, 0, sizeof(*rep));
   rep->outer_steps = 3;
   rep->inner_steps = 123;

@@ -127,7 +127,16 @@ def test_solver_keys_reach_tl_solve(fake_driver, tmp_path):
     assert (s["method"], float(s["rel_tol"]), float(s["inner_tol"]), s["learned"]) == \
         ("2", 1e-11, 0.0, "0")
     assert s["max_inner"] == str(d.max_iters)
+    assert s["projection"] == "0"  # each solve starts from u0 unless asked
     assert "tl_cg_solve" not in _names(calls)
+    # the projected starting guess
+    q = dk.two_state(16, end_step=1)
+    q.extra = ["gb300_solver mixed-learned-coarse", "gb300_projection 7",
+               f"gb300_weights {DEFAULT_RAW_WEIGHTS}"]
+    r, calls = _run(fake_driver, q, tmp_path / "e")
+    assert r.returncode == 0, r.stdout[-1500:]
+    s = _solve_line(calls)
+    assert (s["method"], s["projection"], s["learned"]) == ("5", "7", "1")
     # the environment overrides the deck
     r, calls = _run(fake_driver, d, tmp_path / "b", TL_SOLVER="mixed")
     assert _solve_line(calls)["method"] == "1"
