@@ -25,6 +25,9 @@ the reference's own stop rule sqrt(|rr|) < eps = 1e-15, max_iters 10000
 (`--fp64 fused` for the fused multiply-add contract).
 
 Reported:
+  config     the workload (deck, size, stop rule, timed timesteps): the same
+             object in the reference arm's line
+  solver     the arm's solver, where its solves start, its steps per timestep
   value      device time per timestep (CUDA events on the library's stream,
              inputs resident in HBM; every field is larger than L2)
   e2e        the same K timesteps again, from the same starting state,
@@ -204,34 +207,45 @@ def stop_rule(solver: str) -> str:
     return f"FP64 true residual ||u0 - A u|| <= {REL_TOL:g} ||u0||"
 
 
-def config_for(args, steps_per_timestep=None) -> dict:
+def config_for(args) -> dict:
+    """The workload, the same in both arms: deck, size, stop rule, the timed
+    timesteps. What solves it (and how many steps it took) is the line's
+    `solver` object."""
     deck = ("two-state deck (background rho 100 / e 1e-4, hot rectangle rho 0.1 / e 25)"
             if args.deck == "two-state" else
             f"random-state deck (splitmix64 seed {RANDOM_SEED}: 20-60 rectangles and discs, "
             "rho log-uniform [0.05, 200], e uniform [1e-4, 25])")
-    solver = {"plain": "plain FP64 CG, persistent kernel (run-ahead drop-in)",
-              "cg64": "plain FP64 CG, persistent kernel",
-              "mixed": "FP32 inner CG in FP64 iterative refinement",
-              "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement",
-              "mixed-learned": "FP32 inner PCG with the learned preconditioner "
-                               "(network collapsed to a 17x17 stencil on the tensor cores) "
-                               "in FP64 iterative refinement",
-              "mixed-learned-coarse": "FP32 inner PCG with the learned preconditioner plus "
-                                      "a coarse level (aggregates, dense FP16 inverse of "
-                                      "P^T A P) in FP64 iterative refinement",
-              }[args.solver]
-    return {"workload": f"{deck} at {args.size}x{args.size} cells, {solver}, stop: "
+    return {"workload": f"{deck} at {args.size}x{args.size} cells, each timestep solved to "
                         f"{stop_rule(args.solver)}, consecutive timesteps",
             "cells": args.size * args.size, "halo_depth": 2, "dt": 0.004,
-            "deck": args.deck, "solver": args.solver, "stop": stop_rule(args.solver),
+            "deck": args.deck, "stop": stop_rule(args.solver),
             "max_iters": MAX_ITERS,
-            "start": (f"A-norm best combination of u0 and the last {projection_for(args, args.solver)}"
-                      " solutions of this run (successive right-hand sides)"
-                      if projection_for(args, args.solver) else "u0 (the reference's x0 = b)"),
             "timed_timesteps": [args.warmup + 1, args.warmup + args.steps],
             "l2": "inputs larger than L2 (each FP64 field 134 MB > 129 MB L2)"
-                  if args.size >= 4096 else "fields smaller than L2 at this size",
-            "cg_steps_per_timestep": steps_per_timestep}
+                  if args.size >= 4096 else "fields smaller than L2 at this size"}
+
+
+SOLVER_TEXT = {
+    "plain": "plain FP64 CG, persistent kernel (run-ahead drop-in)",
+    "cg64": "plain FP64 CG, persistent kernel",
+    "mixed": "FP32 inner CG in FP64 iterative refinement",
+    "mixed-jacobi": "FP32 inner Jacobi-PCG in FP64 iterative refinement",
+    "mixed-learned": "FP32 inner PCG with the learned preconditioner (network collapsed to a "
+                     "17x17 stencil on the tensor cores) in FP64 iterative refinement",
+    "mixed-learned-coarse": "FP32 inner PCG with the learned preconditioner plus a coarse "
+                            "level (aggregates, dense FP16 inverse of P^T A P) in FP64 "
+                            "iterative refinement",
+}
+
+
+def solver_for(args, steps_per_timestep) -> dict:
+    """The GPU arm's solver: its name, what it is, where each solve starts,
+    and the solver steps of every timestep (warm-up and timed)."""
+    k = projection_for(args, args.solver)
+    return {"name": args.solver, "description": SOLVER_TEXT[args.solver],
+            "start": (f"A-norm best combination of the last {k} solutions of this run "
+                      "(successive right-hand sides)" if k else "u0 (the reference's x0 = b)"),
+            "steps_per_timestep": steps_per_timestep}
 
 
 # ----------------------------------------------------------------- CPU side
@@ -285,9 +299,12 @@ def run_reference(args, rank: int, world: int) -> None:
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(config_for(args, [s["cg_steps"] for s in warm + timed]),
-                       solver="plain FP64 CG (CPU oracle, restatement of the reference's "
-                              "c_kernels/sycl semantics)"),
+        "config": config_for(args),
+        "solver": {"name": "reference", "description": "plain FP64 CG (CPU oracle, restatement "
+                                                       "of the reference's c_kernels/sycl "
+                                                       "semantics)",
+                   "start": "u0 (the reference's x0 = b)",
+                   "steps_per_timestep": [s["cg_steps"] for s in warm + timed]},
         "iters_per_s": sum(steps) / total,
         "per_timestep_s": [s["s"] for s in timed],
         "summary_last": timed[-1]["summary"] if timed else None,
@@ -539,7 +556,8 @@ def run_ours(args, rank: int, world: int, dist) -> None:
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.solver in ("plain", "cg64") else "f32 inner / f64 outer",
         "data": "synthetic",
-        "config": config_for(args, [p["cg_steps"] for p in warm + per]),
+        "config": config_for(args),
+        "solver": solver_for(args, [p["cg_steps"] for p in warm + per]),
         "e2e": {"value": e2e_mean / world, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8,
                 "steps": args.steps,

@@ -74,8 +74,12 @@ def test_reference_arm_times_the_gpu_arms_window_whole(oracle_built):
     d = json.loads(out.stdout.strip().splitlines()[-1])
     c = oracle_built.OracleChunk(bench.deck_for(64, "random"))
     counts = [c.cg_timestep(rel_tol=bench.REL_TOL) for _ in range(5)]
-    assert d["config"]["cg_steps_per_timestep"] == counts
+    assert d["solver"]["steps_per_timestep"] == counts
     assert d["config"]["timed_timesteps"] == [4, 5]
+    # the workload is the GPU arm's: the same config object
+    assert d["config"] == bench.config_for(type("A", (), {"deck": "random", "size": 64,
+                                                          "solver": "mixed-learned-coarse",
+                                                          "warmup": 3, "steps": 2})())
     assert "whole timesteps 4..5" in d["cpu_baseline"]["sample"]
     assert f"({sum(counts[3:])} CG steps)" in d["cpu_baseline"]["sample"]
     assert d["ms_per_step"] * d["steps"] / 1e3 <= wall
