@@ -8,7 +8,9 @@
  * Launch shapes
  *  - map kernels: 256 threads, one cell per thread, grid-stride;
  *  - reducing kernels: 256 threads (8 warps) per 4096-cell tile, one warp per
- *    64-cell group; the last block to finish reduces the tile partials in
+ *    8 of its 64-cell groups (two cells per lane per group; the five upper
+ *    tree levels of the 8 groups shared out among the lanes,
+ *    warp_sum8_groups); the last block to finish reduces the tile partials in
  *    the reference order and writes the scalar straight into pinned host
  *    memory, so one launch and one stream synchronisation return a dot
  *    product (the reference issues 1 + ceil(log64 n) kernels and a blocking
@@ -99,6 +101,43 @@ int launch_map(tl_context* ctx, const Op& op, int x, int y) {
   return TL_OK;
 }
 
+/* Sums of 8 consecutive 64-cell groups held by one warp, two cells per lane
+ * per group (v[g] = cell 2*lane + cell 2*lane+1 of group g), in the
+ * reference's tree order. Instead of a full butterfly per group (every lane
+ * adding at every level), the warp halves its set of groups at each of the
+ * first three levels (lane pairs exchange the halves they do not keep), then
+ * finishes with two butterfly levels: the same pairs are added at every
+ * level, but each level costs 4, 2, 1, 1, 1 additions per lane instead of 8.
+ * Returns the total of group ((lane&1)<<2 | (lane&2) | (lane>>2&1)); lanes
+ * with equal low three bits hold the same group. */
+__device__ __forceinline__ double warp_sum8_groups(const double v[8], int lane) {
+  const bool h1 = lane & 1, h2 = lane & 2, h4 = lane & 4;
+  double a[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double send = h1 ? v[k] : v[4 + k];
+    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 1);
+    a[k] = (h1 ? v[4 + k] : v[k]) + recv;
+  }
+  double b[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double send = h2 ? a[k] : a[2 + k];
+    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 2);
+    b[k] = (h2 ? a[2 + k] : a[k]) + recv;
+  }
+  const double send = h4 ? b[0] : b[1];
+  const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 4);
+  double c = (h4 ? b[1] : b[0]) + recv;
+  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 8);
+  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 16);
+  return c;
+}
+
+__device__ __forceinline__ int warp_sum8_group_of_lane(int lane) {
+  return ((lane & 1) << 2) | (lane & 2) | ((lane >> 2) & 1);
+}
+
 /* ----------------------------------------------------- reducing kernels */
 
 /* Op must provide `static constexpr int N` (number of sums) and
@@ -119,26 +158,34 @@ reduce_kernel(Op op, int x, int y, int hd, double* part, size_t part_stride,
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const unsigned base = (unsigned)tile * TL_TILE;
-    for (int g = warp; g < TL_GROUP; g += nwarps) {
-      const unsigned i0 = base + (unsigned)g * TL_GROUP + 2u * lane;
-      double c0[N], c1[N];
+    /* each warp: groups g0 .. g0+7 of the tile, the first tree level in the
+     * lane (cells 2*lane, 2*lane+1), the other five shared by the warp */
+    for (int g0 = 8 * warp; g0 < TL_GROUP; g0 += 8 * nwarps) {
+      double v[N][8];
 #pragma unroll
-      for (int s = 0; s < N; ++s) { c0[s] = 0.0; c1[s] = 0.0; }
-      if (i0 < len) {
-        const int jj = (int)(i0 / (unsigned)x);
-        const int kk = (int)(i0 - (unsigned)jj * (unsigned)x);
-        if (interior(kk, jj, x, y, hd)) op(i0, kk, jj, c0);
-      }
-      if (i0 + 1 < len) {
-        const unsigned i1 = i0 + 1;
-        const int jj = (int)(i1 / (unsigned)x);
-        const int kk = (int)(i1 - (unsigned)jj * (unsigned)x);
-        if (interior(kk, jj, x, y, hd)) op(i1, kk, jj, c1);
+      for (int k = 0; k < 8; ++k) {
+        const unsigned i0 = base + (unsigned)(g0 + k) * TL_GROUP + 2u * lane;
+        double c0[N], c1[N];
+#pragma unroll
+        for (int s = 0; s < N; ++s) { c0[s] = 0.0; c1[s] = 0.0; }
+        if (i0 < len) {
+          const int jj = (int)(i0 / (unsigned)x);
+          const int kk = (int)(i0 - (unsigned)jj * (unsigned)x);
+          if (interior(kk, jj, x, y, hd)) op(i0, kk, jj, c0);
+        }
+        if (i0 + 1 < len) {
+          const unsigned i1 = i0 + 1;
+          const int jj = (int)(i1 / (unsigned)x);
+          const int kk = (int)(i1 - (unsigned)jj * (unsigned)x);
+          if (interior(kk, jj, x, y, hd)) op(i1, kk, jj, c1);
+        }
+#pragma unroll
+        for (int s = 0; s < N; ++s) v[s][k] = c0[s] + c1[s];
       }
 #pragma unroll
       for (int s = 0; s < N; ++s) {
-        const double v = tl_tree64(c0[s], c1[s]);
-        if (lane == 0) s_group[s][g] = v;
+        const double t = warp_sum8_groups(v[s], lane);
+        if (lane < 8) s_group[s][g0 + warp_sum8_group_of_lane(lane)] = t;
       }
     }
     __syncthreads();
@@ -657,43 +704,6 @@ struct DiagOp {
       diag[i] = 1.0 + (kx[i + 1] + kx[i]) + (ky[i + x] + ky[i]);
   }
 };
-
-/* Sums of 8 consecutive 64-cell groups held by one warp, two cells per lane
- * per group (v[g] = cell 2*lane + cell 2*lane+1 of group g), in the
- * reference's tree order. Instead of a full butterfly per group (every lane
- * adding at every level), the warp halves its set of groups at each of the
- * first three levels (lane pairs exchange the halves they do not keep), then
- * finishes with two butterfly levels: the same pairs are added at every
- * level, but each level costs 4, 2, 1, 1, 1 additions per lane instead of 8.
- * Returns the total of group ((lane&1)<<2 | (lane&2) | (lane>>2&1)); lanes
- * with equal low three bits hold the same group. */
-__device__ __forceinline__ double warp_sum8_groups(const double v[8], int lane) {
-  const bool h1 = lane & 1, h2 = lane & 2, h4 = lane & 4;
-  double a[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const double send = h1 ? v[k] : v[4 + k];
-    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 1);
-    a[k] = (h1 ? v[4 + k] : v[k]) + recv;
-  }
-  double b[2];
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const double send = h2 ? a[k] : a[2 + k];
-    const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 2);
-    b[k] = (h2 ? a[2 + k] : a[k]) + recv;
-  }
-  const double send = h4 ? b[0] : b[1];
-  const double recv = __shfl_xor_sync(TL_FULL_MASK, send, 4);
-  double c = (h4 ? b[1] : b[0]) + recv;
-  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 8);
-  c = c + __shfl_xor_sync(TL_FULL_MASK, c, 16);
-  return c;
-}
-
-__device__ __forceinline__ int warp_sum8_group_of_lane(int lane) {
-  return ((lane & 1) << 2) | (lane & 2) | ((lane >> 2) & 1);
-}
 
 constexpr int kWarpsPerTile = TL_GROUP / 8;  /* 8 warps x 8 groups = one tile */
 
