@@ -290,13 +290,23 @@ def run_reference(args, rank: int, world: int) -> None:
     cpu = CpuTimesteps(args)
     warm = [cpu.step() for _ in range(args.warmup)]
     t0 = time.perf_counter()
-    timed = [cpu.step() for _ in range(args.steps)]
+    timed = []
+    # whole timesteps W+1..W+K; on a host too slow to finish them within the
+    # budget, the window ends early (at least one timestep) and says so
+    while len(timed) < args.steps:
+        timed.append(cpu.step())
+        if time.perf_counter() - t0 > args.ref_budget:
+            break
     total = time.perf_counter() - t0
-    value = total / args.steps
+    value = total / len(timed)
     steps = [s["cg_steps"] for s in timed]
+    last = args.warmup + len(timed)
+    cut = "" if len(timed) == args.steps else (
+        f"; the window was cut at timestep {last} of {args.warmup + args.steps} by the "
+        f"{args.ref_budget:g} s budget (--ref-budget)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": world, "steps": len(timed), "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_for(args),
@@ -309,9 +319,9 @@ def run_reference(args, rank: int, world: int) -> None:
         "per_timestep_s": [s["s"] for s in timed],
         "summary_last": timed[-1]["summary"] if timed else None,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": "port",
-                         "sample": f"whole timesteps {args.warmup + 1}..{args.warmup + args.steps}"
+                         "sample": f"whole timesteps {args.warmup + 1}..{last}"
                                    f" ({sum(steps)} CG steps), after timesteps 1..{args.warmup}"
-                                   " untimed"},
+                                   f" untimed{cut}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -642,6 +652,9 @@ def main() -> None:
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the other solvers' runs of the same timesteps")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=900.0,
+                    help="reference arm: seconds of timed CPU timesteps before the window is "
+                         "cut short (whole timesteps only)")
     ap.add_argument("--max-iters", type=int, default=10000,
                     help="cap on CG steps per timestep (smaller only for profiling captures)")
     args = ap.parse_args()

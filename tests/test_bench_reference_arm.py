@@ -86,3 +86,15 @@ def test_reference_arm_times_the_gpu_arms_window_whole(oracle_built):
     assert abs(d["iters_per_s"] - sum(counts[3:]) / (d["value"] * d["steps"])) <= \
         1e-9 * d["iters_per_s"]
     assert d["summary_last"] == list(c.summary())
+
+
+def test_reference_arm_budget_cuts_the_window_and_says_so():
+    out = subprocess.run(
+        [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "3",
+         "--warmup", "3", "--size", "64", "--ref-budget", "0"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert d["steps"] == 1
+    assert "whole timesteps 4..4" in d["cpu_baseline"]["sample"]
+    assert "cut at timestep 4 of 6" in d["cpu_baseline"]["sample"]
