@@ -358,7 +358,7 @@ def compare_methods(weights: np.ndarray, size: int, seeds, rel_tol: float = 1e-1
         d = dk.random_deck(size, seed=seed, end_step=1, initial_timestep=timestep)
         for method in out:
             g = GpuChunk(d)
-            net = Net(g.ctx, weights) if method == "mixed-learned" else None
+            net = Net(g.ctx, weights) if method.startswith("mixed-learned") else None
             try:
                 rep = g.solve_timestep(method, rel_tol=rel_tol, learned=net)
                 out[method]["inner_steps"] += rep["inner_steps"]
@@ -395,7 +395,7 @@ def train_cli(argv=None) -> None:
     ap.add_argument("--like", type=int, default=4096,
                     help="harvest with the timestep that gives the problems the rx = dt/dx^2 "
                          "of like^2 problems at dt = 0.004")
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -403,8 +403,9 @@ def train_cli(argv=None) -> None:
     ap.add_argument("--snapshots", default="2,8,32",
                     help="CG step counts at which residuals are harvested")
     ap.add_argument("--noise-fraction", type=float, default=1.0)
-    ap.add_argument("--probe-smoothing", type=float, default=0.0,
-                    help="k: filter the noise probes by a^(-k/2) (0: white noise)")
+    ap.add_argument("--probe-smoothing", type=float, default=1.0,
+                    help="k: filter the noise probes by a^(-k/2) (0: white noise; the "
+                         "committed weights use k = 1)")
     ap.add_argument("--eval-size", type=int, default=1024)
     ap.add_argument("--eval-size-small", type=int, default=512)
     ap.add_argument("--eval-seeds", default="7,8")
@@ -456,7 +457,8 @@ def evaluate_cli(argv=None) -> None:
     Solves one timestep of fresh random-state problems (seeds the network
     was neither trained nor tuned on) to the relative FP64 true residual
     1e-10 with plain FP64 CG (cg64), the FP32-inner CG and Jacobi-PCG in FP64
-    refinement, and the learned PCG in FP64 refinement; prints, per size and
+    refinement, and the learned PCG (without and with the coarse level) in
+    FP64 refinement, each from u0; prints, per size and
     per seed, each method's steps, device time, fall-backs and final
     residual as one JSON line."""
     import argparse
@@ -468,9 +470,10 @@ def evaluate_cli(argv=None) -> None:
                     help="seeds for sizes above 2048 (each plain FP64 CG solve takes seconds)")
     args = ap.parse_args(argv)
     w, meta = load_weights(args.weights)
-    methods = ("cg64", "mixed", "mixed-jacobi", "mixed-learned")
-    result = {"weights": str(args.weights), "rel_tol": 1e-10, "timestep": 0.004,
-              "training": {k: meta.get(k) for k in ("data", "like", "seed0", "steps")},
+    methods = ("cg64", "mixed", "mixed-jacobi", "mixed-learned", "mixed-learned-coarse")
+    result = {"weights": Path(args.weights).name, "rel_tol": 1e-10, "timestep": 0.004,
+              "training": {k: meta.get(k) for k in ("data", "like", "seed0", "steps",
+                                                    "probe_smoothing")},
               "sizes": {}}
     for size in (int(v) for v in args.sizes.split(",")):
         seeds = [int(v) for v in (args.seeds_large if size > 2048 else args.seeds).split(",")]
