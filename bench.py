@@ -652,7 +652,7 @@ def main() -> None:
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the other solvers' runs of the same timesteps")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--ref-budget", type=float, default=900.0,
+    ap.add_argument("--ref-budget", type=float, default=420.0,
                     help="reference arm: seconds of timed CPU timesteps before the window is "
                          "cut short (whole timesteps only)")
     ap.add_argument("--max-iters", type=int, default=10000,
