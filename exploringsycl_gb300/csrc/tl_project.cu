@@ -158,9 +158,10 @@ __global__ void __launch_bounds__(kDotThreads) proj_dots_kernel(int x, int y, in
 
 /* The pass after a solve with the held newest solution X: d = u - X over the
  * interior into dnew; A d by the 5-point operator of TeaLeaf/shared.h:59-63
- * (its diagonal precomputed, fused multiply-adds) applied to the difference (u and X carry the same reflective halos, so d's
- * boundary fluxes vanish as u's do); and d . A d, X . A d and e_k . A d for
- * the kept differences e_k, into out[block][0], [1] and [2 + k]. */
+ * (its diagonal precomputed, fused multiply-adds) applied to the difference
+ * (u and X carry the same reflective halos, so d's boundary fluxes vanish as
+ * u's do); and d . A d, X . A d and e_k . A d for the kept differences e_k,
+ * into out[block][0], [1] and [2 + k]. */
 __global__ void __launch_bounds__(kDotThreads)
 proj_push_kernel(int x, int y, int hd, const double* __restrict__ u, const double* __restrict__ X,
                  const double* __restrict__ kx, const double* __restrict__ ky,
