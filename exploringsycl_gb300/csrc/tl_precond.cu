@@ -109,6 +109,7 @@ constexpr int kLpcgSmem = (kOffTmem + 8 + 127) / 128 * 128;
 /* two-level kernel: the epilogue's restriction sums of the tile row pairs
  * (two tiles in flight x 64 pairs x 2 aggregate columns), then r_c and e_c */
 constexpr int kMaxCoarse = 4096;
+static_assert(kMaxCoarse % kThreads == 0, "coarse vectors are split evenly over a block");
 constexpr int kRestSlots = 8;           /* restriction partials per tile */
 constexpr int kOffRest = kLpcgSmem;
 constexpr int kOffCoarse = kOffRest + 2 * (kTH / 2) * 2 * 4;
@@ -604,14 +605,27 @@ __device__ __forceinline__ float phase_c_gemv(const LpcgParams& P, float* s_rc, 
   const int b = 1 << P.cshift;
   const int arows = b < kTH ? b : kTH, acols = b < kTW ? b : kTW;
   const int ncol = kTW / acols;
-  for (int I = threadIdx.x; I < P.nc; I += blockDim.x) {
-    const int Jc = I / P.ncx, Ic = I - Jc * P.ncx;
-    const int gy = Jc << P.cshift, gx = Ic << P.cshift;
-    const int tile = (gy / kTH) * P.tiles_x + gx / kTW;
-    const int loc = ((gy % kTH) / arows) * ncol + (gx % kTW) / acols;
-    float v = __ldcg(P.rc_part + (size_t)tile * kRestSlots + loc);
-    if (b > kTW) v += __ldcg(P.rc_part + (size_t)(tile + 1) * kRestSlots);
-    s_rc[I] = v;
+  /* kMaxCoarse / kThreads entries per thread, all loads issued before the
+   * first store (one L2 round trip instead of one per entry) */
+  constexpr int kPer = kMaxCoarse / kThreads;
+  float v[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int I = threadIdx.x + k * kThreads;
+    v[k] = 0.0f;
+    if (I < P.nc) {
+      const int Jc = I / P.ncx, Ic = I - Jc * P.ncx;
+      const int gy = Jc << P.cshift, gx = Ic << P.cshift;
+      const int tile = (gy / kTH) * P.tiles_x + gx / kTW;
+      const int loc = ((gy % kTH) / arows) * ncol + (gx % kTW) / acols;
+      v[k] = __ldcg(P.rc_part + (size_t)tile * kRestSlots + loc);
+      if (b > kTW) v[k] += __ldcg(P.rc_part + (size_t)(tile + 1) * kRestSlots);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int I = threadIdx.x + k * kThreads;
+    if (I < P.nc) s_rc[I] = v[k];
   }
   __syncthreads();
   const int rows = (P.nc + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -724,7 +738,20 @@ __device__ __forceinline__ void lpcg_body(const LpcgParams& P, TileState& T, flo
         const float dot = phase_c_gemv(P, s_rc, s_red);
         if (threadIdx.x == 0) part_ce[blockIdx.x] = (double)dot;
         if (!tl_grid_barrier(P.sync, P.status)) return;
-        for (int I = threadIdx.x; I < P.nc; I += blockDim.x) s_ec[I] = __ldcg(P.ec + I);
+        {
+          constexpr int kPer = kMaxCoarse / kThreads;
+          float ev[kPer];
+#pragma unroll
+          for (int q = 0; q < kPer; ++q) {
+            const int I = threadIdx.x + q * kThreads;
+            ev[q] = I < P.nc ? __ldcg(P.ec + I) : 0.0f;
+          }
+#pragma unroll
+          for (int q = 0; q < kPer; ++q) {
+            const int I = threadIdx.x + q * kThreads;
+            if (I < P.nc) s_ec[I] = ev[q];
+          }
+        }
         rz += sum_partials(part_ce, G, s_one);  /* its barrier also publishes s_ec */
       }
     }
