@@ -10,8 +10,8 @@ FP32 inner PCG whose preconditioner is the trained network collapsed
 to one 17x17 stencil (tensor cores) plus a coarse level (64 x 64-cell
 aggregates, the dense inverse of P^T A P, stored as FP16 scaled by a power
 of two, applied every step), inside FP64 iterative refinement, started from
-the A-norm best combination of u0 and the last 7 solutions (successive
-right-hand sides; `--projection 0` starts from u0 as the reference does).
+the A-norm best combination of the last 7 solutions (successive right-hand
+sides; `--projection 0` starts from u0 as the reference does).
 The same timesteps are also solved, under the same stop rule, with plain
 FP64 CG from u0 in both arithmetic contracts (exact / fused multiply-add),
 with the mixed-precision Jacobi-PCG, the learned PCG and the two-level
@@ -33,7 +33,10 @@ Reported:
   e2e        the same K timesteps again, from the same starting state,
              through the C ABI with host buffers: density and energy copied
              in from pinned host memory, energy copied back, inside the
-             timed region (host wall clock, one synchronisation per step)
+             timed region (host wall clock, one synchronisation per step);
+             with the projected guess the held solutions are dropped and
+             timesteps 1..W replayed untimed first, so that the solves start
+             from the same history as the timed ones
   iters_per_s  solver steps (CG or inner PCG steps) per second of `value`
   roofline   the dominant kernel (the persistent inner FP32 kernel of the
              mixed solver, or the FP64 CG kernel for plain/cg64): algorithmic
@@ -51,7 +54,8 @@ Reported:
              started from the GPU's FP64 CG state at the start of the timed
              window, which the oracle would have computed bit for bit
 --impl reference times that CPU path alone through whole timesteps: 1..W
-untimed, W+1..W+K timed (the same window as the GPU arm).
+untimed, W+1..W+K timed (the same window as the GPU arm), cut short at a
+whole timestep after --ref-budget seconds (420 by default) on a slow host.
 
 Multi-GPU: replicas only (one independent chunk per GPU); value is the
 whole-job time per timestep (max over ranks / timesteps of all ranks).
