@@ -80,7 +80,8 @@ def test_tabulated_temperature(n, steps, tmp_path, backend_built):
     assert run.passed is True, run.stdout[-800:]
 
 
-@pytest.mark.parametrize("solver", ["cg64", "mixed", "mixed-jacobi", "mixed-learned"])
+@pytest.mark.parametrize("solver", ["cg64", "mixed", "mixed-jacobi", "mixed-learned",
+                                    "mixed-learned-coarse"])
 def test_solver_replacement_under_the_driver(solver, tmp_path, backend_built, oracle_built):
     """gb300_solver in the deck: the driver loop ends after one pass, the
     backend reports the true solve, and the final temperature agrees with
@@ -98,6 +99,31 @@ def test_solver_replacement_under_the_driver(solver, tmp_path, backend_built, or
     for line in gpu.stdout.splitlines():
         if line.startswith("TL_SOLVE"):
             assert float(line.split("rel_residual=")[1].split()[0]) <= 1e-11
+    tg, tc = gpu.summaries[-1][3], cpu.summaries[-1][3]
+    assert abs(tg - tc) <= 1e-8 * abs(tc)
+
+
+def test_projected_guess_under_the_driver(tmp_path, backend_built, oracle_built):
+    """The bench's headline configuration through the reference driver's
+    timestep loop: gb300_solver mixed-learned-coarse with gb300_projection 7
+    on a 128^2 random-state deck at strong couplings, 8 timesteps. Every
+    solve meets its target, the later ones start from the projected guess
+    (fewer inner steps than the first), and the final temperature agrees
+    with the oracle's plain CG."""
+    from exploringsycl_gb300.learned import DEFAULT_RAW_WEIGHTS
+    d = dk.random_deck(128, seed=51, end_step=8, initial_timestep=0.004 * 1024)
+    d.extra = ["gb300_solver mixed-learned-coarse", "gb300_projection 7",
+               "gb300_rel_tol 1e-11", f"gb300_weights {DEFAULT_RAW_WEIGHTS}"]
+    gpu = run_driver(DRIVER_EXE, d, tmp_path / "gpu")
+    cpu = run_driver(oracle_built.DRIVER, d, tmp_path / "cpu")
+    assert gpu.returncode == 0, gpu.stdout[-2000:]
+    inner = []
+    for line in gpu.stdout.splitlines():
+        if line.startswith("TL_SOLVE"):
+            assert float(line.split("rel_residual=")[1].split()[0]) <= 1e-11, line
+            inner.append(int(line.split("inner=")[1].split()[0]))
+    assert len(inner) == 8
+    assert max(inner[4:]) < inner[0], inner
     tg, tc = gpu.summaries[-1][3], cpu.summaries[-1][3]
     assert abs(tg - tc) <= 1e-8 * abs(tc)
 
