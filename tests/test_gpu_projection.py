@@ -212,3 +212,17 @@ def test_set_up_couplings_follow_density_and_overwrites(backend_built):
     finally:
         a.close()
         b.close()
+
+
+def test_projection_on_a_ragged_grid(backend_built):
+    """A 75 x 90 interior (no dimension a multiple of 4) with the FP32 CG
+    method: the projection's passes cover exactly the interior, and the
+    projected solves keep the solution of the solves from u0."""
+    d = dk.Deck(75, 90, dk.random_states(52), end_step=6, initial_timestep=0.004 * 2048)
+    r0, u0s, _, _, _ = _run(d, "mixed", 6, 0)
+    r4, u4s, _, _, _ = _run(d, "mixed", 6, 4)
+    for r in r0 + r4:
+        assert r["final_rel_residual"] <= 1e-10 and r["fallback_events"] == 0, r
+    assert any(r["projection_basis"] > 0 for r in r4[2:])
+    for a, b in zip(u4s, u0s):
+        assert np.max(np.abs(a - b)) <= 1e-8 * np.max(np.abs(b))
